@@ -1,0 +1,308 @@
+"""Benchmark of the planet SDF -> contour path on GB300.
+
+Workload: the 512^3 torus + 8 spheres planet minus 6-octave ridged Perlin and
+a cellular F2-F1 layer (seed 42, box [-1.6, 1.6]^3): one "step" is one fused
+value + analytic-gradient sampling of the full 512^3 grid (134,217,728
+samples). Also measured in the same run: the plain (value-only) kernel, the
+full planet (sampling + dual contouring) in ms, and the same metric end to
+end through the C ABI with pinned host output buffers.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU path (the oracle's FP32
+restatement, per-sample callback, gradient by 6-tap central differences) on
+the host cores; under torchrun only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SDF+grad Gsamples/s at 512^3 (fused value+gradient; plain and ms/planet alongside)"
+UNIT = "Gsamples/s"
+CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
+
+
+def _pkg():
+    return importlib.import_module("unnatural-planets_gb300")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_rate(P, grid, slabs: int, threads: int, grad: bool) -> tuple[float, float]:
+    """Samples/s of the oracle's FP32 callback path over `slabs` z-slabs from
+    the middle of the grid; returns (rate, seconds)."""
+    from oracle import oracle as O
+    nz = int(grid.n[2])
+    z0 = nz // 2 - slabs // 2
+    t = time.perf_counter()
+    if grad:
+        O.synth_grid_fp32_cd(P, grid, z0, z0 + slabs, CD_TAP, threads)
+    else:
+        O.synth_grid_fp32(P, grid, z0, z0 + slabs, threads)
+    dt = time.perf_counter() - t
+    return int(grid.n[0]) * int(grid.n[1]) * slabs / dt, dt
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_reference(args) -> None:
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    up = _pkg()
+    W = up.workloads
+    P = W.torus_spheres_ridged_cellular()
+    grid = W.grid(W.GRID_C2, n=(args.grid,) * 3)
+    threads = os.cpu_count() or 1
+    slabs = min(max(2 * threads, 16), args.grid)
+    for _ in range(args.warmup):
+        cpu_rate(P, grid, 2, threads, grad=True)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        r, s = cpu_rate(P, grid, slabs, threads, grad=True)
+        rates.append(r)
+        secs.append(s)
+    value = args.steps * slabs * args.grid * args.grid / sum(secs) / 1e9
+    sample = f"{slabs} z-slabs of {args.grid}x{args.grid} ({slabs * args.grid * args.grid} samples) per step, value + 6-tap central-difference gradient (h={CD_TAP})"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded planet program; no dataset)",
+        "config": {"workload": f"torus+8 spheres - ridged perlin 6 oct + cellular F2-F1, seed 42, {args.grid}^3 over [-1.6,1.6]^3"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample, "cpu": _cpu_model()},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    up = _pkg()
+    W = up.workloads
+    P = W.torus_spheres_ridged_cellular()
+    grid = W.grid(W.GRID_C2, n=(args.grid,) * 3)
+    N = grid.count
+    planet = up.Planet(program=P)
+    stream = torch.cuda.current_stream()
+    planet.set_stream(stream.cuda_stream)
+    d = torch.empty(N, device="cuda")
+    g = torch.empty(3 * N, device="cuda")
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, k):
+        """per-step CUDA-event durations on the launching stream (ms)"""
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        barrier()
+        t0 = time.perf_counter()
+        for a, b in evs:
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier()
+        return [a.elapsed_time(b) for a, b in evs], wall
+
+    fused = lambda: planet.sdf_grid(grid, 1, outs=[d, None, None], grad=g)  # noqa: E731
+    plain = lambda: planet.sdf_grid(grid, 1, outs=[d, None, None])  # noqa: E731
+    for _ in range(args.warmup):
+        fused()
+        plain()
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid).replace("GPU-", "")
+    except Exception:
+        gpu_id = str(local)
+    with Clocks(gpu_id) as clk:
+        fused_ms, _ = timed(fused, args.steps)
+    plain_ms, _ = timed(plain, args.steps)
+    t_fused = sum(fused_ms) / len(fused_ms)
+    if ws > 1:
+        t = torch.tensor([t_fused], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_fused = float(t.item())
+    value = ws * N / (t_fused * 1e-3) / 1e9
+    t_plain = sum(plain_ms) / len(plain_ms)
+
+    # full planet: sampling + dual contouring into device buffers
+    pos0, _, idx0 = planet.contour(grid)
+    V, I = len(pos0), len(idx0)
+    pos = torch.empty((V, 3), device="cuda")
+    nrm = torch.empty((V, 3), device="cuda")
+    idx = torch.empty(I, dtype=torch.int32, device="cuda")
+    import ctypes as C
+    mesh = up.abi.MeshOut(pos.data_ptr(), nrm.data_ptr(), idx.data_ptr(), V, I, 0, 0)
+
+    def planet_step():
+        st = planet.lib.up_contour(planet.h, 0, C.byref(grid), None, C.byref(mesh))
+        assert st == 0, st
+    for _ in range(max(1, args.warmup)):
+        planet_step()
+    planet_ms, planet_wall = timed(planet_step, args.steps)
+
+    # end to end through the C ABI with pinned host outputs (D2H inside the timed region)
+    dh = torch.empty(N, pin_memory=True)
+    gh = torch.empty(3 * N, pin_memory=True)
+    e2e_fn = lambda: planet.sdf_grid(grid, 1, outs=[dh, None, None], grad=gh)  # noqa: E731
+    e2e_fn()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_fn()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    barrier()
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return
+    # roofline: FP32-pipe bound kernel; algorithmic FLOPs from the oracle's count
+    flops = W.FLOPS_PER_SAMPLE_C2 * N
+    achieved = flops / (t_fused * 1e-3) / 1e12
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    max_mhz = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = sms * 128 * 2 * max_mhz * 1e6 / 1e12
+    # CPU baseline (rank 0, bounded sample)
+    threads = os.cpu_count() or 1
+    slabs = min(max(2 * threads, 16), args.grid)
+    cpu_grad, cpu_s = cpu_rate(P, grid, slabs, threads, grad=True)
+    cpu_plain, _ = cpu_rate(P, grid, slabs, threads, grad=False)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_fused, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded planet program; no dataset)",
+        "config": {"workload": f"torus+8 spheres - ridged perlin 6 oct + cellular F2-F1, seed 42, {args.grid}^3 over [-1.6,1.6]^3",
+                   "samples_per_step": N, "parallelism": f"replicas x{ws}",
+                   "l2": "no inputs; 2.1 GB of outputs per step (> 129 MB L2)"},
+        "plain_gsamples_s": ws * N / (t_plain * 1e-3) / 1e9, "plain_ms": t_plain,
+        "ms_per_planet": sum(planet_ms) / len(planet_ms),
+        "planet": {"what": f"{args.grid}^3 value sampling + dual contouring (count, emit, Hermite, FP64 QEF, quads) into device buffers",
+                   "vertices": V, "triangles": I // 3},
+        "e2e": {"value": ws * N / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 * N,
+                "what": "up_sdf_grid value+gradient into pinned host buffers"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "traffic": None,
+                     "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x {max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)",
+                     "flops_per_sample": W.FLOPS_PER_SAMPLE_C2,
+                     "note": "value-path FLOPs of the oracle count; the gradient's extra arithmetic and all integer hashing are not counted"},
+        "cpu_baseline": {"value": cpu_grad / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{slabs} z-slabs of {args.grid}x{args.grid} per leg; value+gradient by 6-tap central differences",
+                         "plain_value": cpu_plain / 1e9, "cpu": _cpu_model()},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=512, help="grid edge (512 is the benchmark; smaller for profiling captures)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

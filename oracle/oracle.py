@@ -1,0 +1,150 @@
+"""ctypes wrapper of the oracle library (TEST INFRASTRUCTURE, parity unpinned).
+
+Only the test suite, the smoke check and the CPU-baseline leg of the
+benchmark use this module. It restates the reference's arithmetic on the
+CPU (FP64, per-operation FP32, forward-mode dual numbers) to check the CUDA
+path; it is never the thing measured or shipped.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_LIBS = {}
+
+
+def _pkg_abi():
+    import importlib
+    root = str(HERE.parent)
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    return importlib.import_module("unnatural-planets_gb300.abi")
+
+
+def lib(fast: bool = False) -> C.CDLL:
+    name = "liboracle_fast.so" if fast else "liboracle.so"
+    if name in _LIBS:
+        return _LIBS[name]
+    from . import build_oracle  # noqa: F401  (package-relative when imported as oracle.oracle)
+    build_oracle.build()
+    L = C.CDLL(str(HERE / "_build" / name))
+    abi = _pkg_abi()
+    P = C.POINTER(abi.SynthProgram)
+    G = C.POINTER(abi.Grid)
+    vp = C.c_void_p
+    sigs = {
+        "orc_mix32": (C.c_uint32, [C.c_uint32]),
+        "orc_lattice_hash": (C.c_uint32, [C.c_int32, C.c_int32, C.c_int32, C.c_uint32]),
+        "orc_seed_key": (C.c_uint32, [C.c_uint32]),
+        "orc_noise": (None, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint32, vp,
+                             C.c_uint64, C.c_int, vp, vp]),
+        "orc_synth_theta_count": (C.c_uint64, [P]),
+        "orc_synth_theta": (None, [P, vp]),
+        "orc_synth_points": (None, [P, vp, vp, C.c_uint64, C.c_int, vp, vp, C.c_int]),
+        "orc_synth_theta_grad": (C.c_int, [P, vp, vp, C.c_uint64, vp, vp, C.c_int]),
+        "orc_synth_count_ops": (None, [P, vp, C.c_uint64, vp]),
+        "orc_synth_grid_fp32": (None, [P, G, C.c_uint32, C.c_uint32, vp, C.c_int]),
+        "orc_synth_grid_fp32_cd": (None, [P, G, C.c_uint32, C.c_uint32, C.c_float, vp, vp, C.c_int]),
+        "orc_grid_positions": (None, [G, vp]),
+        "orc_contour_synth": (vp, [P, G, vp]),
+        "orc_mesh_counts": (None, [vp, vp]),
+        "orc_mesh_copy": (None, [vp, vp, vp, vp, vp, vp]),
+        "orc_mesh_free": (None, [vp]),
+    }
+    for n, (res, args) in sigs.items():
+        f = getattr(L, n)
+        f.restype = res
+        f.argtypes = args
+    _LIBS[name] = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def noise(cfg: dict, xyz: np.ndarray, precision: int = 0, grad: bool = False):
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    n = xyz.shape[0]
+    out = np.empty(n, np.float64)
+    g = np.empty((n, 3), np.float64) if grad else None
+    lib().orc_noise(cfg.get("type", 3), cfg.get("fractal", 0), cfg.get("octaves", 3), cfg.get("distance", 0),
+                    cfg.get("operation", 1), cfg.get("frequency", 1.0), cfg.get("lacunarity", 2.0), cfg.get("gain", 0.5),
+                    cfg.get("seed", 0), _p(xyz), n, precision, _p(out), _p(g))
+    return (out, g) if grad else out
+
+
+def synth_points(P, xyz, theta=None, precision=0, grad=False, threads=8):
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    n = xyz.shape[0]
+    out = np.empty(n, np.float64)
+    g = np.empty((n, 3), np.float64) if grad else None
+    th = None if theta is None else np.ascontiguousarray(theta, np.float64)
+    lib().orc_synth_points(C.byref(P), _p(th), _p(xyz), n, precision, _p(out), _p(g), threads)
+    return (out, g) if grad else out
+
+
+def synth_theta(P) -> np.ndarray:
+    n = lib().orc_synth_theta_count(C.byref(P))
+    out = np.empty(n, np.float64)
+    lib().orc_synth_theta(C.byref(P), _p(out))
+    return out
+
+
+def synth_theta_grad(P, xyz, w, theta=None, threads=8) -> np.ndarray:
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    w = np.ascontiguousarray(w, np.float64)
+    n = lib().orc_synth_theta_count(C.byref(P))
+    out = np.empty(n, np.float64)
+    th = None if theta is None else np.ascontiguousarray(theta, np.float64)
+    if lib().orc_synth_theta_grad(C.byref(P), _p(th), _p(xyz), xyz.shape[0], _p(w), _p(out), threads) != 0:
+        raise ValueError("too many parameters")
+    return out
+
+
+def synth_count_ops(P, xyz) -> dict:
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    c = np.zeros(5, np.float64)
+    lib().orc_synth_count_ops(C.byref(P), _p(xyz), xyz.shape[0], _p(c))
+    return dict(flop=c[0], div=c[1], sqrt=c[2], floor=c[3], transcendental=c[4])
+
+
+def synth_grid_fp32(P, grid, z0, z1, threads, fast=True) -> np.ndarray:
+    nx, ny = int(grid.n[0]), int(grid.n[1])
+    out = np.empty(nx * ny * (z1 - z0), np.float32)
+    lib(fast).orc_synth_grid_fp32(C.byref(P), C.byref(grid), z0, z1, _p(out), threads)
+    return out
+
+
+def synth_grid_fp32_cd(P, grid, z0, z1, h, threads, fast=True):
+    nx, ny = int(grid.n[0]), int(grid.n[1])
+    n = nx * ny * (z1 - z0)
+    out = np.empty(n, np.float32)
+    g = np.empty(3 * n, np.float32)
+    lib(fast).orc_synth_grid_fp32_cd(C.byref(P), C.byref(grid), z0, z1, h, _p(out), _p(g), threads)
+    return out, g
+
+
+def grid_positions(grid) -> np.ndarray:
+    out = np.empty((grid.count, 3), np.float32)
+    lib().orc_grid_positions(C.byref(grid), _p(out))
+    return out
+
+
+def contour_synth(P, grid, values: np.ndarray) -> dict:
+    values = np.ascontiguousarray(values, np.float32)
+    h = lib().orc_contour_synth(C.byref(P), C.byref(grid), _p(values))
+    try:
+        c = np.zeros(4, np.uint64)
+        lib().orc_mesh_counts(h, _p(c))
+        V, I, E = int(c[0]), int(c[1]), int(c[2])
+        r = dict(cells=np.empty(V, np.uint64), positions=np.empty((V, 3), np.float32), normals=np.empty((V, 3), np.float32),
+                 indices=np.empty(I, np.uint32), edges=np.empty(E, np.uint64))
+        lib().orc_mesh_copy(h, _p(r["cells"]), _p(r["positions"]), _p(r["normals"]), _p(r["indices"]), _p(r["edges"]))
+        return r
+    finally:
+        lib().orc_mesh_free(h)

@@ -1,0 +1,260 @@
+// C entry points of the oracle for the test suite (ctypes) and the CPU
+// baseline of the benchmark. TEST INFRASTRUCTURE, parity unpinned (see
+// oracle_core.hpp). Nothing in the product links this file.
+#include "oracle_core.hpp"
+#include "oracle_synth.hpp"
+#include "oracle_contour.hpp"
+#include "oracle_modes.hpp"
+
+#include <atomic>
+#include <memory>
+#include <thread>
+#include <vector>
+
+using namespace orc;
+
+namespace {
+
+template<class F>
+void parallel_for(uint64_t n, int threads, F &&f) {
+	if (threads <= 1 || n < 2) { for (uint64_t i = 0; i < n; i++) f(i); return; }
+	std::atomic<uint64_t> next{0};
+	std::vector<std::thread> ts;
+	for (int t = 0; t < threads; t++)
+		ts.emplace_back([&]() {
+			for (;;) {
+				const uint64_t i = next.fetch_add(1);
+				if (i >= n) break;
+				f(i);
+			}
+		});
+	for (auto &t : ts) t.join();
+}
+
+template<class T>
+std::vector<T> theta_as(const up_synth_program &p, const double *theta) {
+	std::vector<double> t0 = synth_theta(p);
+	std::vector<T> t(t0.size());
+	for (size_t i = 0; i < t0.size(); i++) t[i] = T(theta ? theta[i] : t0[i]);
+	return t;
+}
+
+} // namespace
+
+extern "C" {
+
+int orc_abi_version() { return 1; }
+
+uint32_t orc_mix32(uint32_t x) { return mix32(x); }
+uint32_t orc_lattice_hash(int32_t x, int32_t y, int32_t z, uint32_t key) { return lattice_hash(x, y, z, key); }
+uint32_t orc_seed_key(uint32_t seed) { return seed_key(seed); }
+
+// one noise function (NoiseCfg) at n points; precision 0 = FP64, 1 = FP32;
+// grad (3 per point, FP64 dual numbers) when not null
+void orc_noise(int type, int fractal, int octaves, int dist, int op, double frequency, double lacunarity, double gain,
+	uint32_t seed, const float *xyz, uint64_t n, int precision, double *out, double *grad) {
+	NoiseCfg c;
+	c.type = type; c.fractal = fractal; c.octaves = octaves; c.dist = dist; c.op = op;
+	c.frequency = frequency; c.lacunarity = lacunarity; c.gain = gain; c.seed = seed;
+	const NoiseFn fn = make_noise(c);
+	for (uint64_t i = 0; i < n; i++) {
+		const float *q = xyz + 3 * i;
+		if (grad) {
+			V3<Dual<3>> p(Dual<3>::var(q[0], 0), Dual<3>::var(q[1], 1), Dual<3>::var(q[2], 2));
+			Dual<3> v = noise_eval(fn, p);
+			out[i] = v.v;
+			for (int a = 0; a < 3; a++) grad[3 * i + a] = v.d[a];
+		} else if (precision == 1) {
+			out[i] = val(noise_eval(fn, V3<F32>(q[0], q[1], q[2])));
+		} else {
+			out[i] = noise_eval(fn, V3<double>(q[0], q[1], q[2]));
+		}
+	}
+}
+
+uint64_t orc_synth_theta_count(const up_synth_program *p) { return (uint64_t)synth_theta_count(*p); }
+void orc_synth_theta(const up_synth_program *p, double *out) {
+	auto t = synth_theta(*p);
+	for (size_t i = 0; i < t.size(); i++) out[i] = t[i];
+}
+
+// d(p) of a synthetic program at n points; theta may be null (program's own)
+void orc_synth_points(const up_synth_program *prog, const double *theta, const float *xyz, uint64_t n, int precision,
+	double *out, double *grad, int threads) {
+	const up_synth_program P = *prog;
+	if (grad) {
+		auto th = theta_as<Dual<3>>(P, theta);
+		parallel_for(n, threads, [&](uint64_t i) {
+			const float *q = xyz + 3 * i;
+			V3<Dual<3>> p(Dual<3>::var(q[0], 0), Dual<3>::var(q[1], 1), Dual<3>::var(q[2], 2));
+			Dual<3> v = synth_eval(P, th.data(), p);
+			out[i] = v.v;
+			for (int a = 0; a < 3; a++) grad[3 * i + a] = v.d[a];
+		});
+	} else if (precision == 1) {
+		auto th = theta_as<F32>(P, theta);
+		parallel_for(n, threads, [&](uint64_t i) {
+			const float *q = xyz + 3 * i;
+			out[i] = val(synth_eval(P, th.data(), V3<F32>(q[0], q[1], q[2])));
+		});
+	} else {
+		auto th = theta_as<double>(P, theta);
+		parallel_for(n, threads, [&](uint64_t i) {
+			const float *q = xyz + 3 * i;
+			out[i] = synth_eval(P, th.data(), V3<double>(q[0], q[1], q[2]));
+		});
+	}
+}
+
+// dtheta = sum_i w_i dd(p_i)/dtheta (FP64 forward-mode, up to 40 parameters)
+int orc_synth_theta_grad(const up_synth_program *prog, const double *theta, const float *xyz, uint64_t n,
+	const double *w, double *dtheta, int threads) {
+	constexpr int K = 40;
+	const up_synth_program P = *prog;
+	const int nt = synth_theta_count(P);
+	if (nt > K) return 1;
+	std::vector<double> t0 = synth_theta(P);
+	const int nth = std::max(threads, 1);
+	std::vector<std::vector<double>> part(nth, std::vector<double>(nt, 0.0));
+	const uint64_t chunk = (n + nth - 1) / nth;
+	parallel_for((uint64_t)nth, nth, [&](uint64_t t) {
+		std::vector<Dual<K>> th(nt);
+		for (int j = 0; j < nt; j++) th[j] = Dual<K>::var(theta ? theta[j] : t0[j], j);
+		for (uint64_t i = t * chunk; i < std::min(n, (t + 1) * chunk); i++) {
+			const float *q = xyz + 3 * i;
+			Dual<K> v = synth_eval(P, th.data(), V3<Dual<K>>(Dual<K>(q[0]), Dual<K>(q[1]), Dual<K>(q[2])));
+			for (int j = 0; j < nt; j++) part[t][j] += w[i] * v.d[j];
+		}
+	});
+	for (int j = 0; j < nt; j++) {
+		double s = 0;
+		for (int t = 0; t < nth; t++) s += part[t][j];
+		dtheta[j] = s;
+	}
+	return 0;
+}
+
+// algorithmic operation counts per sample, averaged over n points
+void orc_synth_count_ops(const up_synth_program *prog, const float *xyz, uint64_t n, double *counts5) {
+	const up_synth_program P = *prog;
+	auto th = theta_as<Counted>(P, nullptr);
+	opcounts() = OpCounts();
+	for (uint64_t i = 0; i < n; i++) {
+		const float *q = xyz + 3 * i;
+		(void)synth_eval(P, th.data(), V3<Counted>(q[0], q[1], q[2]));
+	}
+	const OpCounts c = opcounts();
+	counts5[0] = (double)c.flop / n; counts5[1] = (double)c.div / n; counts5[2] = (double)c.sqrt / n;
+	counts5[3] = (double)c.floor / n; counts5[4] = (double)c.transc / n;
+}
+
+// ---------------------------------------------------------------- CPU baseline
+// The reference samples its SDF through a per-sample callback
+// (Delegate<Real(const Vec3&)>, sources/meshGeneration.cpp:39). The baseline
+// keeps that structure: an FP32 function pointer called once per sample,
+// parallel over z-slabs on `threads` host threads.
+namespace {
+const up_synth_program *g_cb_prog = nullptr;
+std::vector<F32> g_cb_theta;
+float synth_callback(const float p[3]) { return (float)val(synth_eval(*g_cb_prog, g_cb_theta.data(), V3<F32>(p[0], p[1], p[2]))); }
+}
+
+// samples z-slabs [z0, z1) of the grid into out (nx*ny*(z1-z0) floats)
+void orc_synth_grid_fp32(const up_synth_program *prog, const up_grid *grid, uint32_t z0, uint32_t z1, float *out, int threads) {
+	g_cb_prog = prog;
+	g_cb_theta = theta_as<F32>(*prog, nullptr);
+	float (*const volatile fn)(const float *) = &synth_callback;
+	const GridF g(*grid);
+	const uint64_t nx = g.n[0], ny = g.n[1];
+	parallel_for((uint64_t)(z1 - z0), threads, [&](uint64_t kz) {
+		const uint32_t k = z0 + (uint32_t)kz;
+		float p[3];
+		p[2] = g.coord(2, k);
+		for (uint64_t j = 0; j < ny; j++) {
+			p[1] = g.coord(1, (uint32_t)j);
+			for (uint64_t i = 0; i < nx; i++) {
+				p[0] = g.coord(0, (uint32_t)i);
+				out[(kz * ny + j) * nx + i] = fn(p);
+			}
+		}
+	});
+}
+
+// Same, plus the gradient by 6-tap central differences (tap distance h):
+// the reference-side way of obtaining contouring normals that the analytic
+// gradient replaces. grad receives 3 planes of nx*ny*(z1-z0) floats.
+void orc_synth_grid_fp32_cd(const up_synth_program *prog, const up_grid *grid, uint32_t z0, uint32_t z1, float h, float *out, float *grad,
+	int threads) {
+	g_cb_prog = prog;
+	g_cb_theta = theta_as<F32>(*prog, nullptr);
+	float (*const volatile fn)(const float *) = &synth_callback;
+	const GridF g(*grid);
+	const uint64_t nx = g.n[0], ny = g.n[1];
+	const uint64_t plane = nx * ny * (uint64_t)(z1 - z0);
+	const float inv = 0.5f / h;
+	parallel_for((uint64_t)(z1 - z0), threads, [&](uint64_t kz) {
+		const uint32_t k = z0 + (uint32_t)kz;
+		float p[3], q[3];
+		p[2] = g.coord(2, k);
+		for (uint64_t j = 0; j < ny; j++) {
+			p[1] = g.coord(1, (uint32_t)j);
+			for (uint64_t i = 0; i < nx; i++) {
+				p[0] = g.coord(0, (uint32_t)i);
+				const uint64_t idx = (kz * ny + j) * nx + i;
+				out[idx] = fn(p);
+				for (int a = 0; a < 3; a++) {
+					q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+					q[a] = p[a] + h;
+					const float fp = fn(q);
+					q[a] = p[a] - h;
+					const float fm = fn(q);
+					grad[a * plane + idx] = (fp - fm) * inv;
+				}
+			}
+		}
+	});
+}
+
+// grid sample positions (3 floats per sample) exactly as the FP32 path forms them
+void orc_grid_positions(const up_grid *grid, float *out) {
+	const GridF g(*grid);
+	uint64_t idx = 0;
+	for (uint32_t k = 0; k < g.n[2]; k++)
+		for (uint32_t j = 0; j < g.n[1]; j++)
+			for (uint32_t i = 0; i < g.n[0]; i++) {
+				out[3 * idx] = g.coord(0, i); out[3 * idx + 1] = g.coord(1, j); out[3 * idx + 2] = g.coord(2, k);
+				idx++;
+			}
+}
+
+// ---------------------------------------------------------------- contour
+struct OrcMesh { ContourResult r; };
+
+static GradFn synth_gradfn(const up_synth_program *prog) {
+	auto P = std::make_shared<up_synth_program>(*prog);
+	auto th = std::make_shared<std::vector<Dual<3>>>(theta_as<Dual<3>>(*prog, nullptr));
+	return [P, th](const double p[3], double g[3]) {
+		V3<Dual<3>> q(Dual<3>::var(p[0], 0), Dual<3>::var(p[1], 1), Dual<3>::var(p[2], 2));
+		Dual<3> v = synth_eval(*P, th->data(), q);
+		for (int a = 0; a < 3; a++) g[a] = v.d[a];
+	};
+}
+
+void *orc_contour_synth(const up_synth_program *prog, const up_grid *grid, const float *values) {
+	auto *m = new OrcMesh();
+	contour(*grid, values, synth_gradfn(prog), m->r);
+	return m;
+}
+
+void orc_mesh_counts(void *h, uint64_t *c4) {
+	auto *m = (OrcMesh *)h;
+	c4[0] = m->r.cells.size(); c4[1] = m->r.indices.size(); c4[2] = m->r.edges.size(); c4[3] = 0;
+}
+void orc_mesh_copy(void *h, uint64_t *cells, float *positions, float *normals, uint32_t *indices, uint64_t *edges) {
+	auto *m = (OrcMesh *)h;
+	auto cp = [](auto &v, auto *dst) { if (dst) std::copy(v.begin(), v.end(), dst); };
+	cp(m->r.cells, cells); cp(m->r.positions, positions); cp(m->r.normals, normals); cp(m->r.indices, indices); cp(m->r.edges, edges);
+}
+void orc_mesh_free(void *h) { delete (OrcMesh *)h; }
+
+} // extern "C"

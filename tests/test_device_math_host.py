@@ -1,0 +1,81 @@
+"""The CUDA path's device arithmetic headers (csrc/*.cuh), compiled as host
+C++ by tests/hostcheck, against the FP64 oracle: every noise type with its
+analytic gradient, both synthetic programs, and the parameter adjoint. This
+checks arithmetic without a GPU; the kernels are checked in the gpu tests."""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import abi as _abi, workloads
+
+sys.path.insert(0, str(Path(__file__).parent / "hostcheck"))
+import build_hostcheck  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def H():
+    L = C.CDLL(str(build_hostcheck.build()))
+    abi = _abi()
+    vp = C.c_void_p
+    L.hc_noise.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, vp, C.c_uint64, vp, vp]
+    L.hc_synth.argtypes = [C.POINTER(abi.SynthProgram), vp, C.c_uint64, vp, vp]
+    L.hc_synth_bwd.argtypes = [C.POINTER(abi.SynthProgram), vp, C.c_uint64, vp, vp]
+    L.hc_synth_bwd.restype = C.c_int
+    L.hc_lattice_hash.restype = C.c_uint32
+    L.hc_lattice_hash.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32]
+    L.hc_corner_hash.restype = C.c_uint32
+    L.hc_corner_hash.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int]
+    return L
+
+
+def test_hash_bit_exact(H, O):
+    r = np.random.default_rng(0)
+    L = O.lib()
+    for x, y, z, k in r.integers(-2 ** 31, 2 ** 31 - 2, size=(2000, 4)):
+        k = int(k) & 0xFFFFFFFF
+        h = L.orc_lattice_hash(int(x), int(y), int(z), k)
+        assert H.hc_lattice_hash(int(x), int(y), int(z), k) == h
+        # the shared-product corner form equals the direct hash for all 8 corners
+        for b in range(8):
+            assert H.hc_corner_hash(int(x), int(y), int(z), k, b) == L.orc_lattice_hash(
+                int(x) + (b & 1), int(y) + ((b >> 1) & 1), int(z) + (b >> 2), k)
+
+
+CASES = [(t, 0, 1) for t in range(5)] + [(5, d, op) for d in range(3) for op in range(7)]
+
+
+@pytest.mark.parametrize("t,dist,op", CASES)
+def test_noise_value_and_gradient(H, O, t, dist, op):
+    x = np.random.default_rng(t * 31 + dist * 7 + op).uniform(-20, 20, size=(5000, 3)).astype(np.float32)
+    key = O.lib().orc_seed_key(11)
+    out = np.empty(len(x), np.float32)
+    g = np.empty((len(x), 3), np.float32)
+    H.hc_noise(t, dist, op, key, x.ctypes.data, len(x), out.ctypes.data, g.ctypes.data)
+    ref, rg = O.noise(dict(type=t, seed=11, distance=dist, operation=op), x, grad=True)
+    # FP32 evaluation of coordinates up to |20|: position rounding ~1e-6
+    assert np.abs(out - ref).max() < 5e-5
+    assert np.abs(g - rg).max() < 5e-4 * (1 + np.abs(rg).max())
+
+
+@pytest.mark.parametrize("which", ["c1", "c2"])
+def test_synth_value_gradient_adjoint(H, O, which):
+    W = workloads()
+    P = W.sphere_fbm() if which == "c1" else W.torus_spheres_ridged_cellular()
+    xs = np.random.default_rng(2).uniform(-1.5, 1.5, size=(5000, 3)).astype(np.float32)
+    out = np.empty(len(xs), np.float32)
+    g = np.empty((len(xs), 3), np.float32)
+    H.hc_synth(C.byref(P), xs.ctypes.data, len(xs), out.ctypes.data, g.ctypes.data)
+    ref, rg = O.synth_points(P, xs, grad=True)
+    assert np.abs(out - ref).max() < 1e-5
+    assert np.abs(g - rg).max() < 1e-4
+    w = np.random.default_rng(3).normal(size=len(xs)).astype(np.float32)
+    dt = np.zeros(64)
+    m = H.hc_synth_bwd(C.byref(P), xs.ctypes.data, len(xs), w.ctypes.data, dt.ctypes.data)
+    rt = O.synth_theta_grad(P, xs, w.astype(np.float64))
+    assert m == len(rt)
+    np.testing.assert_allclose(dt[:m], rt, rtol=1e-4, atol=1e-3)

@@ -1,0 +1,439 @@
+// C ABI implementation: contexts, host/device buffer staging, error
+// reporting, and the orchestration of the SDF, contouring, texel and batch
+// kernels. Every entry point catches C++ exceptions and returns a status.
+#include "up_internal.h"
+#include "up_modes_desc.h"
+#include "up_noise.cuh"
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace up {
+int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
+uint32_t instance_seed(uint32_t seed, uint32_t slot);
+cudaError_t launch_modes_grid(const ModesDesc &M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
+	unsigned *nanflag, cudaStream_t s);
+cudaError_t launch_modes_points(const ModesDesc &M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag,
+	cudaStream_t s);
+} // namespace up
+
+using namespace up;
+
+enum BufSlot {
+	B_IN0, B_OUT0, B_OUT1, B_OUT2, B_GRAD, B_GRID, B_PARTIALS, B_W,
+	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN,
+	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
+	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
+	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
+	B_COUNT
+};
+
+struct up_context {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	bool synthetic = false;
+	up_synth_program prog{};
+	ModesDesc modes{};
+	std::string shape_name;
+	bool double_sided = false;
+	std::string last_error;
+	unsigned *d_flag = nullptr;
+	struct Buf { void *p = nullptr; size_t n = 0; } bufs[B_COUNT];
+};
+
+namespace {
+
+std::atomic<up_context *> g_current{nullptr};
+
+struct Fail {
+	int code;
+	std::string msg;
+};
+
+int fail(up_context *ctx, int code, const std::string &msg) {
+	if (ctx) ctx->last_error = msg;
+	return code;
+}
+
+void check(cudaError_t e, const char *what) {
+	if (e == cudaSuccess) return;
+	if (e == cudaErrorMemoryAllocation) throw Fail{UP_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e)};
+	throw Fail{UP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+void *buf(up_context *ctx, int slot, size_t bytes) {
+	auto &b = ctx->bufs[slot];
+	if (bytes == 0) bytes = 16;
+	if (b.n >= bytes) return b.p;
+	if (b.p) check(cudaFree(b.p), "cudaFree");
+	b.p = nullptr;
+	b.n = 0;
+	size_t want = bytes + bytes / 8;
+	check(cudaMalloc(&b.p, want), "cudaMalloc");
+	b.n = want;
+	return b.p;
+}
+
+bool is_device(const void *p) {
+	if (!p) return false;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// device view of a caller input: the pointer itself, or a staged copy
+const void *stage_in(up_context *ctx, int slot, const void *p, size_t bytes) {
+	if (is_device(p)) return p;
+	void *d = buf(ctx, slot, bytes);
+	check(cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync H2D");
+	return d;
+}
+// device target for a caller output: the pointer itself, or scratch
+void *stage_out(up_context *ctx, int slot, void *p, size_t bytes) {
+	if (!p) return nullptr;
+	if (is_device(p)) return p;
+	return buf(ctx, slot, bytes);
+}
+void finish_out(up_context *ctx, void *host, const void *dev, size_t bytes) {
+	if (!host || host == dev) return;
+	check(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync D2H");
+}
+
+void set_device(up_context *ctx) { check(cudaSetDevice(ctx->device), "cudaSetDevice"); }
+
+void reset_flag(up_context *ctx) { check(cudaMemsetAsync(ctx->d_flag, 0, sizeof(unsigned), ctx->stream), "cudaMemsetAsync"); }
+unsigned read_flag(up_context *ctx) {
+	unsigned f = 0;
+	check(cudaMemcpyAsync(&f, ctx->d_flag, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync flag");
+	check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+	return f;
+}
+
+const char *field_word(int field) {
+	switch (field) {
+		case UP_FIELD_LAND: return "land";
+		case UP_FIELD_WATER: return "water";
+		case UP_FIELD_NAVIGATION: return "navigation";
+		case UP_FIELD_ELEVATION: return "elevation";
+		default: return "elevation raw";
+	}
+}
+
+int init_context(up_context *ctx) {
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+		cudaGetLastError();
+		return UP_ERR_NO_DEVICE;
+	}
+	check(cudaGetDevice(&ctx->device), "cudaGetDevice");
+	check(cudaMalloc(&ctx->d_flag, 16), "cudaMalloc flag");
+	return UP_OK;
+}
+
+template<class F>
+int guarded(up_context *ctx, F &&f) {
+	try {
+		return f();
+	} catch (const Fail &e) {
+		return fail(ctx, e.code, e.msg);
+	} catch (const std::bad_alloc &) {
+		return fail(ctx, UP_ERR_OOM, "host allocation failed");
+	} catch (const std::exception &e) {
+		return fail(ctx, UP_ERR_CUDA, e.what());
+	} catch (...) {
+		return fail(ctx, UP_ERR_CUDA, "unknown error");
+	}
+}
+
+bool valid_grid(const up_grid *g) {
+	if (!g) return false;
+	for (int a = 0; a < 3; a++) {
+		if (g->n[a] < 2) return false;
+		if (!(g->hi[a] > g->lo[a])) return false;
+	}
+	const uint64_t n = (uint64_t)g->n[0] * g->n[1] * g->n[2];
+	return n < (1ull << 31);
+}
+
+bool valid_program(const up_synth_program &p) {
+	if (p.base < 0 || p.base > 3 || p.n_layers < 0 || p.n_layers > 2 || p.n_spheres < 0 || p.n_spheres > 8) return false;
+	for (int l = 0; l < p.n_layers; l++) {
+		const up_noise_layer &L = p.layer[l];
+		if (L.type < 0 || L.type > 5 || L.fractal < 0 || L.fractal > 2 || L.octaves < 1 || L.octaves > 8) return false;
+		if (L.distance < 0 || L.distance > 2 || L.operation < 0 || L.operation > 6) return false;
+	}
+	return true;
+}
+
+} // namespace
+
+// ============================================================================
+extern "C" {
+
+const char *up_status_string(int s) {
+	switch (s) {
+		case UP_OK: return "ok";
+		case UP_ERR_INVALID_ARGUMENT: return "invalid argument";
+		case UP_ERR_INVALID_MODE: return "invalid mode";
+		case UP_ERR_NAN: return "invalid sdf value";
+		case UP_ERR_OOM: return "out of memory";
+		case UP_ERR_CUDA: return "cuda error";
+		case UP_ERR_CAPACITY: return "insufficient capacity";
+		case UP_ERR_TIMEOUT: return "timeout";
+		case UP_ERR_EMPTY_MESH: return "empty mesh";
+		case UP_ERR_NO_DEVICE: return "no cuda device";
+		default: return "unknown status";
+	}
+}
+
+const char *up_last_error(const up_context *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+uint32_t up_instance_seed(uint32_t seed, uint32_t slot) { return instance_seed(seed, slot); }
+
+size_t up_synth_theta_count(const up_synth_program *p) {
+	if (!p) return 0;
+	size_t n = 0;
+	for (int l = 0; l < p->n_layers && l < 2; l++) n += 2 * (size_t)p->layer[l].octaves;
+	switch (p->base) {
+		case UP_BASE_SPHERE: n += 1; break;
+		case UP_BASE_TORUS: case UP_BASE_ROUNDED_BOX: n += 2; break;
+		default: n += 3 + (size_t)p->n_spheres;
+	}
+	return n;
+}
+
+int up_context_create(const up_modes *modes, const up_seeds *seeds, up_context **out) {
+	if (!modes || !out) return UP_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	up_context *ctx = new (std::nothrow) up_context();
+	if (!ctx) return UP_ERR_OOM;
+	std::string err;
+	const int st = build_modes(*modes, seeds ? seeds->seed : 0u, ctx->modes, ctx->shape_name, ctx->double_sided, err);
+	if (st != UP_OK) {
+		delete ctx;
+		return st;
+	}
+	const int r = guarded(ctx, [&]() { return init_context(ctx); });
+	if (r != UP_OK) {
+		delete ctx;
+		return r;
+	}
+	*out = ctx;
+	return UP_OK;
+}
+
+int up_context_create_synthetic(const up_synth_program *program, up_context **out) {
+	if (!program || !out) return UP_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	if (!valid_program(*program)) return UP_ERR_INVALID_ARGUMENT;
+	up_context *ctx = new (std::nothrow) up_context();
+	if (!ctx) return UP_ERR_OOM;
+	ctx->synthetic = true;
+	ctx->prog = *program;
+	ctx->shape_name = "synthetic";
+	const int r = guarded(ctx, [&]() { return init_context(ctx); });
+	if (r != UP_OK) {
+		delete ctx;
+		return r;
+	}
+	*out = ctx;
+	return UP_OK;
+}
+
+int up_context_destroy(up_context *ctx) {
+	if (!ctx) return UP_ERR_INVALID_ARGUMENT;
+	up_context *expect = ctx;
+	g_current.compare_exchange_strong(expect, nullptr);
+	cudaSetDevice(ctx->device);
+	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+	for (auto &b : ctx->bufs) if (b.p) cudaFree(b.p);
+	if (ctx->d_flag) cudaFree(ctx->d_flag);
+	delete ctx;
+	return UP_OK;
+}
+
+int up_context_set_stream(up_context *ctx, void *stream) {
+	if (!ctx) return UP_ERR_INVALID_ARGUMENT;
+	ctx->stream = (cudaStream_t)stream;
+	return UP_OK;
+}
+
+int up_context_shape_name(const up_context *ctx, char *b, size_t n) {
+	if (!ctx || !b || n == 0) return UP_ERR_INVALID_ARGUMENT;
+	std::snprintf(b, n, "%s", ctx->shape_name.c_str());
+	return ctx->shape_name.size() < n ? UP_OK : UP_ERR_CAPACITY;
+}
+
+int up_context_double_sided(const up_context *ctx) { return ctx && ctx->double_sided ? 1 : 0; }
+
+int up_context_set_theta(up_context *ctx, const float *theta, size_t n) {
+	if (!ctx || !theta || !ctx->synthetic) return UP_ERR_INVALID_ARGUMENT;
+	up_synth_program &p = ctx->prog;
+	if (n != up_synth_theta_count(&p)) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "theta size mismatch");
+	size_t t = 0;
+	for (int l = 0; l < p.n_layers; l++) {
+		for (int i = 0; i < p.layer[l].octaves; i++) p.layer[l].amp[i] = theta[t++];
+		for (int i = 0; i < p.layer[l].octaves; i++) p.layer[l].freq[i] = theta[t++];
+	}
+	switch (p.base) {
+		case UP_BASE_SPHERE: p.param[0] = theta[t++]; break;
+		case UP_BASE_TORUS: case UP_BASE_ROUNDED_BOX: p.param[0] = theta[t++]; p.param[1] = theta[t++]; break;
+		default:
+			p.param[0] = theta[t++]; p.param[1] = theta[t++];
+			for (int s = 0; s < p.n_spheres; s++) p.sphere[s][3] = theta[t++];
+			p.k = theta[t++];
+	}
+	return UP_OK;
+}
+
+int up_set_current_context(up_context *ctx) {
+	g_current.store(ctx);
+	return UP_OK;
+}
+
+int up_sdf_eval_points(up_context *ctx, int field, const float *xyz, size_t n, float *d, float *grad) {
+	if (!ctx || !xyz || !d || n == 0) return UP_ERR_INVALID_ARGUMENT;
+	if (field < 0 || field > 4) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "bad field");
+	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const float *dx = (const float *)stage_in(ctx, B_IN0, xyz, n * 12);
+		float *dd = (float *)stage_out(ctx, B_OUT0, d, n * 4);
+		float *dg = (float *)stage_out(ctx, B_GRAD, grad, n * 12);
+		reset_flag(ctx);
+		if (ctx->synthetic) check(launch_synth_points(ctx->prog, dx, n, dd, dg, ctx->d_flag, ctx->stream), "sdf points kernel");
+		else check(launch_modes_points(ctx->modes, field, dx, n, dd, dg, ctx->d_flag, ctx->stream), "sdf points kernel");
+		finish_out(ctx, d, dd, n * 4);
+		finish_out(ctx, grad, dg, n * 12);
+		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
+		return (int)UP_OK;
+	});
+}
+
+static float shim(int field, const float p[3]) {
+	up_context *ctx = g_current.load();
+	if (!ctx || !p) return NAN;
+	float d = NAN;
+	if (up_sdf_eval_points(ctx, field, p, 1, &d, nullptr) != UP_OK) return NAN;
+	return d;
+}
+float up_sdf_land(const float p[3]) { return shim(UP_FIELD_LAND, p); }
+float up_sdf_water(const float p[3]) { return shim(UP_FIELD_WATER, p); }
+float up_sdf_navigation(const float p[3]) { return shim(UP_FIELD_NAVIGATION, p); }
+
+int up_sdf_grid(up_context *ctx, uint32_t mask, const up_grid *grid, float *const out[3], float *grad) {
+	if (!ctx || !valid_grid(grid) || !out) return UP_ERR_INVALID_ARGUMENT;
+	mask &= 7u;
+	if (!mask) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "empty fields mask");
+	if (ctx->synthetic && mask != 1u) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
+	for (int f = 0; f < 3; f++)
+		if ((mask >> f & 1u) && !out[f]) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "missing output for a selected field");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const GridDev g = make_grid(*grid);
+		const size_t n = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
+		float *o[3] = {nullptr, nullptr, nullptr};
+		for (int f = 0; f < 3; f++)
+			if (mask >> f & 1u) o[f] = (float *)stage_out(ctx, B_OUT0 + f, out[f], n * 4);
+		float *dg = (float *)stage_out(ctx, B_GRAD, grad, n * 12);
+		reset_flag(ctx);
+		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, g, o[0], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		else check(launch_modes_grid(ctx->modes, mask, g, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		for (int f = 0; f < 3; f++)
+			if (mask >> f & 1u) finish_out(ctx, out[f], o[f], n * 4);
+		finish_out(ctx, grad, dg, n * 12);
+		if (read_flag(ctx)) {
+			int f = 0;
+			while (!(mask >> f & 1u)) f++;
+			return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(f) + " sdf value");
+		}
+		return (int)UP_OK;
+	});
+}
+
+int up_contour(up_context *ctx, int field, const up_grid *grid, const float *values, up_mesh_out *mesh) {
+	if (!ctx || !valid_grid(grid) || !mesh) return UP_ERR_INVALID_ARGUMENT;
+	if (field < 0 || field > 2) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "contour field must be LAND, WATER or NAVIGATION");
+	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const GridDev g = make_grid(*grid);
+		const size_t np = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
+		const size_t nc = (size_t)(grid->n[0] - 1) * (grid->n[1] - 1) * (grid->n[2] - 1);
+		const float *d;
+		if (values) {
+			d = (const float *)stage_in(ctx, B_GRID, values, np * 4);
+		} else {
+			float *gd = (float *)buf(ctx, B_GRID, np * 4);
+			reset_flag(ctx);
+			if (ctx->synthetic) check(launch_synth_grid(ctx->prog, g, gd, nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+			else {
+				float *o[3] = {nullptr, nullptr, nullptr};
+				o[field] = gd;
+				check(launch_modes_grid(ctx->modes, 1u << field, g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+			}
+			if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
+			d = gd;
+		}
+		DcScratch S;
+		const uint32_t nb = dc_num_blocks(g);
+		S.blk_counts = (uint32_t *)buf(ctx, B_DC_BLK, (size_t)nb * 12);
+		S.totals = (uint32_t *)buf(ctx, B_DC_TOT, 16);
+		S.cell_map = (uint32_t *)buf(ctx, B_DC_CMAP, nc * 4);
+		S.edge_map = (uint32_t *)buf(ctx, B_DC_EMAP, np * 12);
+		check(dc_count(d, g, S, ctx->stream), "contour count");
+		uint32_t tot[4] = {0, 0, 0, 0};
+		check(cudaMemcpyAsync(tot, S.totals, 12, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync totals");
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		const uint32_t ncells = tot[0], nedges = tot[1], nquads = tot[2];
+		mesh->vertex_count = ncells;
+		mesh->index_count = 6ull * nquads;
+		if (nquads == 0) return fail(ctx, UP_ERR_EMPTY_MESH, std::string("generated empty base ") + field_word(field) + " mesh");
+		if (!mesh->positions || !mesh->indices || mesh->vertex_capacity < ncells || mesh->index_capacity < 6ull * nquads)
+			return fail(ctx, UP_ERR_CAPACITY, "mesh buffers too small");
+		S.cell_list = (uint32_t *)buf(ctx, B_DC_CLIST, (size_t)ncells * 4);
+		S.edge_list = (uint32_t *)buf(ctx, B_DC_ELIST, (size_t)nedges * 4);
+		S.quad_list = (uint32_t *)buf(ctx, B_DC_QLIST, (size_t)nquads * 4);
+		S.edge_t = (double *)buf(ctx, B_DC_ET, (size_t)nedges * 8);
+		S.edge_n = (float *)buf(ctx, B_DC_EN, (size_t)nedges * 12);
+		check(dc_emit(d, g, S, ctx->stream), "contour emit");
+		float *pos = (float *)stage_out(ctx, B_MESH_POS, mesh->positions, (size_t)ncells * 12);
+		float *nrm = (float *)stage_out(ctx, B_MESH_NRM, mesh->normals, (size_t)ncells * 12);
+		uint32_t *idx = (uint32_t *)stage_out(ctx, B_MESH_IDX, mesh->indices, (size_t)nquads * 24);
+		if (ctx->synthetic) check(dc_geometry_synth(ctx->prog, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
+		else check(dc_geometry_modes(ctx->modes, field, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
+		finish_out(ctx, mesh->positions, pos, (size_t)ncells * 12);
+		finish_out(ctx, mesh->normals, nrm, (size_t)ncells * 12);
+		finish_out(ctx, mesh->indices, idx, (size_t)nquads * 24);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta) {
+	if (!ctx || !points || !dL_dd || !dtheta || n == 0) return UP_ERR_INVALID_ARGUMENT;
+	if (!ctx->synthetic) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "the parameter adjoint needs a synthetic context");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const size_t nt = up_synth_theta_count(&ctx->prog);
+		const float *dp = (const float *)stage_in(ctx, B_IN0, points, n * 12);
+		const float *dw = (const float *)stage_in(ctx, B_W, dL_dd, n * 4);
+		float *dt = (float *)stage_out(ctx, B_OUT0, dtheta, nt * 4);
+		const int nb = synth_bwd_blocks(n);
+		float *part = (float *)buf(ctx, B_PARTIALS, (size_t)nb * 43 * 4);
+		check(launch_synth_bwd(ctx->prog, dp, n, dw, part, nb, dt, ctx->stream), "adjoint kernel");
+		finish_out(ctx, dtheta, dt, nt * 4);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+} // extern "C"

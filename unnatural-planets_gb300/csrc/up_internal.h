@@ -1,0 +1,57 @@
+// Internal host-side interface between the C ABI (up_abi.cu) and the kernel
+// translation units. Not part of the public boundary.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "../../include/up_abi.h"
+
+namespace up {
+
+struct GridDev {
+	float lo[3], step[3];
+	uint32_t n[3];
+};
+GridDev make_grid(const up_grid &g);
+
+// Reference-mode planet description (defined in up_modes.cuh)
+struct ModesDesc;
+
+// ---- SDF sampling (up_sdf.cu / up_modes.cu)
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s);
+cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
+cudaError_t launch_modes_grid(const ModesDesc &M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag, cudaStream_t s);
+cudaError_t launch_modes_points(const ModesDesc &M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
+
+// adjoint: partial sums per block into partials (nblocks x ACC stride), then
+// a fixed-order reduction into dtheta (compact layout)
+int synth_bwd_blocks(uint64_t n);
+cudaError_t launch_synth_bwd(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *partials, int nblocks,
+	float *dtheta, cudaStream_t s);
+
+// ---- dual contouring (up_contour.cu)
+struct DcScratch {
+	uint32_t *blk_counts;   // 3 * nblocks
+	uint32_t *totals;       // 4 (device)
+	uint32_t *cell_map;     // cells
+	uint32_t *edge_map;     // 3 * points
+	uint32_t *cell_list;    // capacity cells
+	uint32_t *edge_list;    // capacity edges
+	uint32_t *quad_list;    // capacity quads
+	double *edge_t;         // capacity edges
+	float *edge_n;          // 3 * capacity edges
+};
+uint32_t dc_num_blocks(const GridDev &g);
+// pass 1: counts -> totals[0]=cells, [1]=edges, [2]=quads (device), returns after enqueue
+cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s);
+// pass 2 (after the host knows the totals and sized the lists)
+cudaError_t dc_emit(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s);
+cudaError_t dc_geometry_synth(const up_synth_program &P, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells, uint32_t nedges,
+	uint32_t nquads, float *pos, float *nrm, uint32_t *idx, cudaStream_t s);
+cudaError_t dc_geometry_modes(const ModesDesc &M, int field, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells,
+	uint32_t nedges, uint32_t nquads, float *pos, float *nrm, uint32_t *idx, cudaStream_t s);
+
+// occupancy-derived persistent grid size
+int persistent_blocks(const void *kernel, int threads, size_t smem = 0);
+
+} // namespace up

@@ -1,0 +1,190 @@
+// SDF sampling kernels for synthetic programs: grid (value or fused
+// value+gradient), scattered points, and the parameter adjoint.
+//
+// Replaces the reference's per-sample callback loop
+// MarchingCubes::updateByPosition(terrainSdf*) (sources/meshGeneration.cpp:39)
+// for the unit-scale synthetic planets. One thread per sample in a
+// grid-stride loop sized from the occupancy of the kernel (a multiple of the
+// SM count); the noise octaves run in registers; stores are coalesced 4-byte
+// writes to x-fastest planes.
+#include "up_internal.h"
+#include "up_synth.cuh"
+
+namespace up {
+
+GridDev make_grid(const up_grid &g) {
+	GridDev d;
+	for (int a = 0; a < 3; a++) {
+		d.lo[a] = g.lo[a];
+		d.n[a] = g.n[a];
+		d.step[a] = (g.hi[a] - g.lo[a]) / (float)(g.n[a] - 1);
+	}
+	return d;
+}
+
+int persistent_blocks(const void *kernel, int threads, size_t smem) {
+	int dev = 0, sms = 0, per = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1) per = 1;
+	return sms * per;
+}
+
+__device__ __forceinline__ float grid_coord(const GridDev &g, int a, uint32_t i) {
+	return __fadd_rn(__fmul_rn((float)i, g.step[a]), g.lo[a]);
+}
+
+template<bool GRAD, int T0, int T1>
+__global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
+	float *__restrict__ grad, unsigned *__restrict__ nanflag) {
+	const uint32_t nx = g.n[0], ny = g.n[1];
+	const uint64_t plane = (uint64_t)nx * ny * g.n[2];
+	const uint32_t total = (uint32_t)plane;
+	bool bad = false;
+	for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+		const uint32_t i = idx % nx, r = idx / nx, j = r % ny, k = r / ny;
+		const V3f p = v3(grid_coord(g, 0, i), grid_coord(g, 1, j), grid_coord(g, 2, k));
+		const NG d = synth_eval<GRAD, T0, T1>(P, p);
+		out[idx] = d.v;
+		if (GRAD) {
+			grad[idx] = d.g.x;
+			grad[plane + idx] = d.g.y;
+			grad[2 * plane + idx] = d.g.z;
+		}
+		bad |= isnan(d.v);
+	}
+	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
+}
+
+template<bool GRAD, int T0, int T1>
+__global__ void __launch_bounds__(256) synth_points_kernel(const up_synth_program P, const float *__restrict__ xyz, uint64_t n,
+	float *__restrict__ out, float *__restrict__ grad, unsigned *__restrict__ nanflag) {
+	bool bad = false;
+	for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (uint64_t)gridDim.x * blockDim.x) {
+		const V3f p = v3(xyz[3 * idx], xyz[3 * idx + 1], xyz[3 * idx + 2]);
+		const NG d = synth_eval<GRAD, T0, T1>(P, p);
+		out[idx] = d.v;
+		if (GRAD) {
+			grad[3 * idx] = d.g.x;
+			grad[3 * idx + 1] = d.g.y;
+			grad[3 * idx + 2] = d.g.z;
+		}
+		bad |= isnan(d.v);
+	}
+	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
+}
+
+// Specialisations: the two benchmark programs get compile-time noise types;
+// everything else dispatches on the layer type at run time.
+enum Spec { SPEC_PERLIN_CELL = 0, SPEC_SIMPLEX = 1, SPEC_GENERIC = 2 };
+constexpr int CELL_EU_SUB = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);
+static Spec spec_of(const up_synth_program &P) {
+	if (P.n_layers == 2 && P.layer[0].type == UP_NOISE_PERLIN && P.layer[1].type == UP_NOISE_CELLULAR &&
+		P.layer[1].distance == UP_DIST_EUCLIDEAN && P.layer[1].operation == UP_OP_SUBTRACT)
+		return SPEC_PERLIN_CELL;
+	if (P.n_layers == 1 && P.layer[0].type == UP_NOISE_SIMPLEX) return SPEC_SIMPLEX;
+	return SPEC_GENERIC;
+}
+
+template<class K, class... A>
+static cudaError_t launch_persistent(K kernel, uint64_t work, cudaStream_t s, A... args) {
+	const int threads = 256;
+	int blocks = persistent_blocks((const void *)kernel, threads);
+	const uint64_t need = (work + threads - 1) / threads;
+	if ((uint64_t)blocks > need) blocks = (int)(need > 0 ? need : 1);
+	kernel<<<blocks, threads, 0, s>>>(args...);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s) {
+	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
+	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
+	const Spec sp = spec_of(P);
+	if (grad) {
+		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag);
+		if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<true, 3, -1>, n, s, P, g, out, grad, nanflag);
+		return launch_persistent(synth_grid_kernel<true, -1, -1>, n, s, P, g, out, grad, nanflag);
+	}
+	if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<false, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag);
+	if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<false, 3, -1>, n, s, P, g, out, grad, nanflag);
+	return launch_persistent(synth_grid_kernel<false, -1, -1>, n, s, P, g, out, grad, nanflag);
+}
+
+cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s) {
+	const Spec sp = spec_of(P);
+	if (grad) {
+		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_points_kernel<true, 2, CELL_EU_SUB>, n, s, P, xyz, n, d, grad, nanflag);
+		if (sp == SPEC_SIMPLEX) return launch_persistent(synth_points_kernel<true, 3, -1>, n, s, P, xyz, n, d, grad, nanflag);
+		return launch_persistent(synth_points_kernel<true, -1, -1>, n, s, P, xyz, n, d, grad, nanflag);
+	}
+	if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_points_kernel<false, 2, CELL_EU_SUB>, n, s, P, xyz, n, d, grad, nanflag);
+	if (sp == SPEC_SIMPLEX) return launch_persistent(synth_points_kernel<false, 3, -1>, n, s, P, xyz, n, d, grad, nanflag);
+	return launch_persistent(synth_points_kernel<false, -1, -1>, n, s, P, xyz, n, d, grad, nanflag);
+}
+
+// ---------------------------------------------------------------- adjoint
+constexpr int BWD_THREADS = 256;
+
+template<int T0, int T1>
+__global__ void __launch_bounds__(BWD_THREADS) synth_bwd_kernel(const up_synth_program P, const float *__restrict__ xyz, uint64_t n,
+	const float *__restrict__ w, float *__restrict__ partials) {
+	float acc[ACC_N];
+	#pragma unroll
+	for (int i = 0; i < ACC_N; i++) acc[i] = 0.f;
+	for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (uint64_t)gridDim.x * blockDim.x) {
+		const V3f p = v3(xyz[3 * idx], xyz[3 * idx + 1], xyz[3 * idx + 2]);
+		synth_bwd<T0, T1>(P, p, w[idx], acc);
+	}
+	// warp sums, then warps in a fixed order: deterministic per block
+	__shared__ float red[BWD_THREADS / 32][ACC_N];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	#pragma unroll
+	for (int i = 0; i < ACC_N; i++) {
+		float v = acc[i];
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+		if (lane == 0) red[wid][i] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x < ACC_N) {
+		float v = 0.f;
+		#pragma unroll
+		for (int k = 0; k < BWD_THREADS / 32; k++) v += red[k][threadIdx.x];
+		partials[(uint64_t)blockIdx.x * ACC_N + threadIdx.x] = v;
+	}
+}
+
+struct SlotMap { int slot[64]; int n; };
+
+// one block: each thread owns theta entries, sums the block partials in order
+__global__ void synth_bwd_reduce(const float *__restrict__ partials, int nblocks, const SlotMap m, float *__restrict__ dtheta) {
+	for (int t = threadIdx.x; t < m.n; t += blockDim.x) {
+		const int s = m.slot[t];
+		double v = 0.0;
+		for (int b = 0; b < nblocks; b++) v += partials[(uint64_t)b * ACC_N + s];
+		dtheta[t] = (float)v;
+	}
+}
+
+int synth_bwd_blocks(uint64_t n) {
+	int blocks = persistent_blocks((const void *)synth_bwd_kernel<-1, -1>, BWD_THREADS);
+	const uint64_t need = (n + BWD_THREADS - 1) / BWD_THREADS;
+	if ((uint64_t)blocks > need) blocks = (int)(need > 0 ? need : 1);
+	return blocks;
+}
+
+cudaError_t launch_synth_bwd(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *partials, int nblocks,
+	float *dtheta, cudaStream_t s) {
+	const Spec sp = spec_of(P);
+	if (sp == SPEC_PERLIN_CELL) synth_bwd_kernel<2, CELL_EU_SUB><<<nblocks, BWD_THREADS, 0, s>>>(P, xyz, n, w, partials);
+	else if (sp == SPEC_SIMPLEX) synth_bwd_kernel<3, -1><<<nblocks, BWD_THREADS, 0, s>>>(P, xyz, n, w, partials);
+	else synth_bwd_kernel<-1, -1><<<nblocks, BWD_THREADS, 0, s>>>(P, xyz, n, w, partials);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	SlotMap m;
+	m.n = theta_slots(P, m.slot);
+	synth_bwd_reduce<<<1, 64, 0, s>>>(partials, nblocks, m, dtheta);
+	return cudaGetLastError();
+}
+
+} // namespace up

@@ -1,0 +1,224 @@
+// Synthetic unit-scale planet programs (include/up_abi.h, up_synth_program):
+// fused value + analytic gradient, and the per-point parameter adjoint.
+//
+// d(p) = base(p) - sum_layers sum_i amp_i s(n_i(freq_i p)), s = n or 1 - 2|n|
+// The smooth union is the reference's polynomial smoothMin
+// (sources/math.cpp:28-33); the composition "shape minus elevation" follows
+// terrainSdfLand (sources/modesConfiguration.cpp:248-258) at unit scale.
+#pragma once
+#include "up_noise.cuh"
+#include "../../include/up_abi.h"
+
+namespace up {
+
+// Layer noise spec for kernel specialisation: -1 = everything at run time;
+// 0..4 = that noise type; cellular = 5 | (distance + 1) << 4 | (operation + 1) << 8
+constexpr int cell_spec(int dist, int op) { return 5 | ((dist + 1) << 4) | ((op + 1) << 8); }
+
+template<bool GRAD, int TYPE>
+UP_HD NG noise_t(const up_noise_layer &L, V3f q, uint32_t key) {
+	if (TYPE >= 0 && (TYPE & 15) == 5) return cellular_n<GRAD, ((TYPE >> 4) & 15) - 1, ((TYPE >> 8) & 15) - 1>(q, key, L.distance, L.operation);
+	const int t = TYPE >= 0 ? TYPE : L.type;
+	if (TYPE == 2 || (TYPE < 0 && t == 2)) { if (GRAD) return perlin_g(q, key); return ngc(perlin_v(q, key)); }
+	if (TYPE == 3 || (TYPE < 0 && t == 3)) return simplex_n<GRAD, false>(q, key);
+	if (TYPE < 0 && t == 5) return cellular_n<GRAD>(q, key, L.distance, L.operation);
+	return noise_single<GRAD>(t, q, key, L.distance, L.operation);
+}
+
+// one layer: value and gradient with respect to p
+template<bool GRAD, int TYPE>
+UP_HD NG layer_eval(const up_noise_layer &L, V3f p) {
+	float v = 0.f;
+	V3f g = zero3();
+	const bool ridged = L.fractal == UP_FRACTAL_RIDGED;
+	#pragma unroll 1
+	for (int i = 0; i < L.octaves; i++) {
+		const float f = L.freq[i];
+		const NG n = noise_t<GRAD, TYPE>(L, p * f, seed_key(L.seed + (uint32_t)i));
+		float s = n.v, ds = 1.f;
+		if (ridged) { s = 1.f - 2.f * fabsf(n.v); ds = n.v > 0.f ? -2.f : (n.v < 0.f ? 2.f : 0.f); }
+		v += L.amp[i] * s;
+		if (GRAD) g += n.g * (L.amp[i] * ds * f);
+	}
+	return ng(v, g);
+}
+
+// polynomial smooth minimum with partials (sources/math.cpp:28-33)
+struct SMin { float s, da, db, dk; };
+// ik = 1 / k, hoisted by the callers
+UP_HD SMin smooth_min_d(float a, float b, float k, float ik) {
+	const float u = (b - a) * ik * 0.5f + 0.5f;
+	const float h = saturatef(u);
+	SMin r;
+	r.s = b + (a - b) * h - k * h * (1.f - h);
+	const float S = (a - b) - k * (1.f - 2.f * h);
+	const bool in = u > 0.f && u < 1.f;
+	const float dha = in ? -0.5f * ik : 0.f;
+	const float dhk = in ? -(b - a) * 0.5f * ik * ik : 0.f;
+	r.da = h + S * dha;
+	r.db = (1.f - h) - S * dha;
+	r.dk = -h * (1.f - h) + S * dhk;
+	return r;
+}
+
+UP_HD NG torus_d(V3f p, float R, float r) {
+	const float a = sqrtf(p.x * p.x + p.y * p.y);
+	const float qx = a - R, qz = p.z;
+	const float ql = sqrtf(qx * qx + qz * qz);
+	const float ia = a > 0.f ? 1.f / a : 0.f, iq = ql > 0.f ? 1.f / ql : 0.f;
+	return ng(ql - r, v3(qx * iq * p.x * ia, qx * iq * p.y * ia, qz * iq));
+}
+UP_HD NG sphere_d(V3f p, V3f c, float r) {
+	const V3f d = p - c;
+	const float l = length(d);
+	return ng(l - r, l > 0.f ? d * (1.f / l) : zero3());
+}
+UP_HD NG box_d(V3f p, float h, float rr) {
+	const V3f q = v3(fabsf(p.x) - h, fabsf(p.y) - h, fabsf(p.z) - h);
+	const V3f m = v3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
+	const float ml = length(m);
+	const float mx = fmaxf(q.x, fmaxf(q.y, q.z));
+	const V3f sg = v3(p.x >= 0.f ? 1.f : -1.f, p.y >= 0.f ? 1.f : -1.f, p.z >= 0.f ? 1.f : -1.f);
+	V3f g;
+	if (ml > 0.f) g = v3(sg.x * m.x, sg.y * m.y, sg.z * m.z) * (1.f / ml);
+	else if (q.x >= q.y && q.x >= q.z) g = v3(sg.x, 0.f, 0.f);
+	else if (q.y >= q.z) g = v3(0.f, sg.y, 0.f);
+	else g = v3(0.f, 0.f, sg.z);
+	return ng(ml + fminf(mx, 0.f) - rr, g);
+}
+
+template<bool GRAD>
+UP_HD NG synth_base(const up_synth_program &P, V3f p) {
+	switch (P.base) {
+		case UP_BASE_SPHERE: return sphere_d(p, zero3(), P.param[0]);
+		case UP_BASE_TORUS: return torus_d(p, P.param[0], P.param[1]);
+		case UP_BASE_ROUNDED_BOX: return box_d(p, P.param[0], P.param[1]);
+		default: {
+			NG b = torus_d(p, P.param[0], P.param[1]);
+			const float ik = 1.f / P.k;
+			#pragma unroll 1
+			for (int s = 0; s < P.n_spheres; s++) {
+				const NG sd = sphere_d(p, v3(P.sphere[s][0], P.sphere[s][1], P.sphere[s][2]), P.sphere[s][3]);
+				const SMin m = smooth_min_d(b.v, sd.v, P.k, ik);
+				b = ng(m.s, b.g * m.da + sd.g * m.db);
+			}
+			return b;
+		}
+	}
+}
+
+// full program; T0/T1 = compile-time noise type of layer 0/1 (-1 = runtime)
+template<bool GRAD, int T0, int T1>
+UP_HD NG synth_eval(const up_synth_program &P, V3f p) {
+	NG d = synth_base<GRAD>(P, p);
+	if (P.n_layers > 0) {
+		const NG e = layer_eval<GRAD, T0>(P.layer[0], p);
+		d.v -= e.v;
+		if (GRAD) d.g -= e.g;
+	}
+	if (P.n_layers > 1) {
+		const NG e = layer_eval<GRAD, T1>(P.layer[1], p);
+		d.v -= e.v;
+		if (GRAD) d.g -= e.g;
+	}
+	return d;
+}
+
+// ---------------------------------------------------------------- adjoint
+// Fixed accumulator layout (compile-time register indices):
+//   [0,8)  layer0 amp   [8,16)  layer0 freq
+//   [16,24) layer1 amp  [24,32) layer1 freq
+//   [32]   R or h, [33] r or rr, [34,42) sphere radii, [42] k
+constexpr int ACC_N = 43;
+
+template<int TYPE, int SLOT>
+UP_HD void layer_bwd(const up_noise_layer &L, V3f p, float w, float acc[ACC_N]) {
+	const bool ridged = L.fractal == UP_FRACTAL_RIDGED;
+	#pragma unroll
+	for (int i = 0; i < 8; i++) {
+		if (i < L.octaves) {
+			const float f = L.freq[i];
+			const NG n = noise_t<true, TYPE>(L, p * f, seed_key(L.seed + (uint32_t)i));
+			float s = n.v, ds = 1.f;
+			if (ridged) { s = 1.f - 2.f * fabsf(n.v); ds = n.v > 0.f ? -2.f : (n.v < 0.f ? 2.f : 0.f); }
+			acc[SLOT * 16 + i] -= w * s;
+			acc[SLOT * 16 + 8 + i] -= w * L.amp[i] * ds * dot(n.g, p);
+		}
+	}
+}
+
+template<int T0, int T1>
+UP_HD void synth_bwd(const up_synth_program &P, V3f p, float w, float acc[ACC_N]) {
+	if (P.n_layers > 0) layer_bwd<T0, 0>(P.layer[0], p, w, acc);
+	if (P.n_layers > 1) layer_bwd<T1, 1>(P.layer[1], p, w, acc);
+	switch (P.base) {
+		case UP_BASE_SPHERE: acc[32] -= w; break;
+		case UP_BASE_TORUS: {
+			const float a = sqrtf(p.x * p.x + p.y * p.y), qx = a - P.param[0];
+			const float ql = sqrtf(qx * qx + p.z * p.z);
+			acc[32] -= w * (ql > 0.f ? qx / ql : 0.f);
+			acc[33] -= w;
+			break;
+		}
+		case UP_BASE_ROUNDED_BOX: {
+			const float h = P.param[0];
+			const V3f q = v3(fabsf(p.x) - h, fabsf(p.y) - h, fabsf(p.z) - h);
+			const V3f m = v3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
+			const float ml = length(m);
+			acc[32] -= w * (ml > 0.f ? (m.x + m.y + m.z) / ml : 1.f);
+			acc[33] -= w;
+			break;
+		}
+		default: {
+			// forward: keep every intermediate union value, then sweep back
+			float bv[9];
+			const float R = P.param[0];
+			const float a = sqrtf(p.x * p.x + p.y * p.y), qx = a - R;
+			const float ql = sqrtf(qx * qx + p.z * p.z);
+			bv[0] = ql - P.param[1];
+			float sdv[8];
+			const float ik = 1.f / P.k;
+			#pragma unroll
+			for (int s = 0; s < 8; s++) {
+				if (s < P.n_spheres) {
+					const V3f d = p - v3(P.sphere[s][0], P.sphere[s][1], P.sphere[s][2]);
+					sdv[s] = length(d) - P.sphere[s][3];
+					bv[s + 1] = smooth_min_d(bv[s], sdv[s], P.k, ik).s;
+				}
+			}
+			float gb = w; // dL/d(current union value)
+			#pragma unroll
+			for (int s = 7; s >= 0; s--) {
+				if (s < P.n_spheres) {
+					const SMin m = smooth_min_d(bv[s], sdv[s], P.k, ik);
+					acc[34 + s] -= gb * m.db; // d sd / d radius = -1
+					acc[42] += gb * m.dk;
+					gb *= m.da;
+				}
+			}
+			acc[32] -= gb * (ql > 0.f ? qx / ql : 0.f);
+			acc[33] -= gb;
+		}
+	}
+}
+
+// compact theta index -> accumulator slot (host helper, same order as
+// up_synth_theta_count's layout)
+inline int theta_slots(const up_synth_program &P, int *slots) {
+	int n = 0;
+	for (int l = 0; l < P.n_layers; l++) {
+		for (int i = 0; i < P.layer[l].octaves; i++) slots[n++] = l * 16 + i;
+		for (int i = 0; i < P.layer[l].octaves; i++) slots[n++] = l * 16 + 8 + i;
+	}
+	switch (P.base) {
+		case UP_BASE_SPHERE: slots[n++] = 32; break;
+		case UP_BASE_TORUS: case UP_BASE_ROUNDED_BOX: slots[n++] = 32; slots[n++] = 33; break;
+		default:
+			slots[n++] = 32; slots[n++] = 33;
+			for (int s = 0; s < P.n_spheres; s++) slots[n++] = 34 + s;
+			slots[n++] = 42;
+	}
+	return n;
+}
+
+} // namespace up

@@ -1,0 +1,132 @@
+"""Synthetic planet workloads (seeded, unit scale).
+
+Planet programs of the benchmark configurations. Amplitudes are per octave:
+a_i = amp * gain^i / sum_j gain^j (the FBM normalisation divides by the sum
+of the octave gains, so `amp` is the peak displacement), frequencies
+f_i = freq * lacunarity^i. All random draws use numpy's PCG64 generator
+(numpy.random.default_rng), which is stable across platforms.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import abi
+
+
+def _layer(L: abi.NoiseLayer, type_, fractal, octaves, freq, amp, seed, gain=0.5, lac=2.0, distance=0, operation=1):
+    L.type = type_
+    L.fractal = fractal
+    L.octaves = octaves
+    L.distance = distance
+    L.operation = operation
+    L.seed = seed
+    bound = sum(abs(gain) ** i for i in range(octaves)) if fractal != abi.FRACTAL_NONE else 1.0
+    for i in range(8):
+        L.amp[i] = amp * gain ** i / bound if i < octaves else 0.0
+        L.freq[i] = freq * lac ** i if i < octaves else 0.0
+
+
+def sphere_fbm(R=1.0, octaves=4, freq=2.0, lac=2.0, gain=0.5, amp=0.05, seed=1337, noise=abi.NOISE_SIMPLEX) -> abi.SynthProgram:
+    """Unit sphere minus an FBM displacement (the CPU-runnable plain method)."""
+    P = abi.SynthProgram()
+    P.base = abi.BASE_SPHERE
+    P.param[0] = R
+    P.n_layers = 1
+    _layer(P.layer[0], noise, abi.FRACTAL_FBM, octaves, freq, amp, seed, gain, lac)
+    return P
+
+
+def torus_spheres_ridged_cellular(seed=42) -> abi.SynthProgram:
+    """Torus (1.0, 0.4) smooth-unioned (k = 0.1) with 8 spheres (centres
+    U[-1,1]^3, radii U[0.1,0.3]) minus 6-octave ridged Perlin (freq 3, gain 0.5,
+    amp 0.04) plus a cellular F2-F1 layer (freq 8, amp 0.02; Euclidean)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-1.0, 1.0, size=(8, 3))
+    radii = rng.uniform(0.1, 0.3, size=8)
+    P = abi.SynthProgram()
+    P.base = abi.BASE_TORUS_SPHERES
+    P.param[0] = 1.0
+    P.param[1] = 0.4
+    P.n_spheres = 8
+    for s in range(8):
+        for a in range(3):
+            P.sphere[s][a] = float(centres[s, a])
+        P.sphere[s][3] = float(radii[s])
+    P.k = 0.1
+    P.n_layers = 2
+    _layer(P.layer[0], abi.NOISE_PERLIN, abi.FRACTAL_RIDGED, 6, 3.0, 0.04, seed)
+    _layer(P.layer[1], abi.NOISE_CELLULAR, abi.FRACTAL_NONE, 1, 8.0, 0.02, seed + 8, distance=abi.DIST_EUCLIDEAN,
+           operation=abi.OP_SUBTRACT)
+    return P
+
+
+def mixed_planet(rng: np.random.Generator) -> abi.SynthProgram:
+    """One planet of the batched-chunk set: sphere R=1, torus (1.0, 0.4) or
+    rounded cube (half-extent 0.8, rounding 0.1), 4-6 octave simplex or
+    Perlin FBM (freq 2, gain 0.5, amp 0.05)."""
+    P = abi.SynthProgram()
+    kind = int(rng.integers(0, 3))
+    if kind == 0:
+        P.base = abi.BASE_SPHERE
+        P.param[0] = 1.0
+    elif kind == 1:
+        P.base = abi.BASE_TORUS
+        P.param[0] = 1.0
+        P.param[1] = 0.4
+    else:
+        P.base = abi.BASE_ROUNDED_BOX
+        P.param[0] = 0.8
+        P.param[1] = 0.1
+    P.n_layers = 1
+    octaves = int(rng.integers(4, 7))
+    noise = abi.NOISE_SIMPLEX if rng.integers(0, 2) == 0 else abi.NOISE_PERLIN
+    _layer(P.layer[0], noise, abi.FRACTAL_FBM, octaves, 2.0, 0.05, int(rng.integers(0, 2 ** 31)))
+    return P
+
+
+# grids of the configurations
+GRID_C1 = dict(lo=(-1.3, -1.3, -1.3), hi=(1.3, 1.3, 1.3), n=(128, 128, 128))
+GRID_C2 = dict(lo=(-1.6, -1.6, -1.6), hi=(1.6, 1.6, 1.6), n=(512, 512, 512))
+
+
+def grid(spec: dict, n=None) -> abi.Grid:
+    return abi.Grid.make(spec["lo"], spec["hi"], n or spec["n"])
+
+
+def theta_count(P: abi.SynthProgram) -> int:
+    n = sum(2 * P.layer[l].octaves for l in range(P.n_layers))
+    return n + {abi.BASE_SPHERE: 1, abi.BASE_TORUS: 2, abi.BASE_ROUNDED_BOX: 2}.get(P.base, 3 + P.n_spheres)
+
+
+def theta_of(P: abi.SynthProgram) -> np.ndarray:
+    """The differentiable parameter vector (layout of up_synth_program)."""
+    t = []
+    for l in range(P.n_layers):
+        L = P.layer[l]
+        t += [L.amp[i] for i in range(L.octaves)]
+        t += [L.freq[i] for i in range(L.octaves)]
+    if P.base == abi.BASE_SPHERE:
+        t += [P.param[0]]
+    elif P.base in (abi.BASE_TORUS, abi.BASE_ROUNDED_BOX):
+        t += [P.param[0], P.param[1]]
+    else:
+        t += [P.param[0], P.param[1]] + [P.sphere[s][3] for s in range(P.n_spheres)] + [P.k]
+    return np.asarray(t, dtype=np.float32)
+
+
+def shell_points(P_radius: float, thickness: float, n: int, seed: int) -> np.ndarray:
+    """n points uniform in the spherical shell |p| in [R - t, R + t]."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r0, r1 = P_radius - thickness, P_radius + thickness
+    r = np.cbrt(rng.uniform(r0 ** 3, r1 ** 3, size=n))
+    return (d * r[:, None]).astype(np.float32)
+
+
+# Algorithmic FP32 operations per sample of torus_spheres_ridged_cellular(),
+# value path, counted by the oracle's operation-counting scalar over 20000
+# uniform samples of GRID_C2's box (add/sub/mul/min/max/abs/select = 1, so an
+# FMA counts 2; besides these, 8 divisions, 37 square roots and 21 floors per
+# sample are counted apart and not included). Checked by tests/test_oracle.py.
+FLOPS_PER_SAMPLE_C2 = 960.8
