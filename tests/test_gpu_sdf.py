@@ -6,11 +6,6 @@ discontinuities (cellular F1/F2 swaps, ridged creases), where FP32 and FP64
 may evaluate opposite sides: at most 1e-4 of the samples may differ there.
 The oracle evaluates at the exact FP32 sample positions the CUDA path forms."""
 
-
-def grad_ok(g, ref):
-    tol = 1e-4 * max(1.0, float(np.abs(ref).max()))
-    bad = np.abs(np.asarray(g) - ref).max(axis=1) > tol
-    return bad.mean() <= 1e-4
 from __future__ import annotations
 
 import numpy as np
@@ -19,6 +14,12 @@ import pytest
 from conftest import workloads
 
 pytestmark = pytest.mark.gpu
+
+
+def grad_ok(g, ref):
+    tol = 1e-4 * max(1.0, float(np.abs(ref).max()))
+    bad = np.abs(np.asarray(g) - ref).max(axis=1) > tol
+    return bad.mean() <= 1e-4
 
 
 def _programs():
