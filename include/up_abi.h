@@ -260,6 +260,21 @@ int up_tiles(up_context *ctx, int purpose, const float *positions, const float *
  * reference counterpart. */
 int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta);
 
+/* Allocation-free variant of up_sdf_param_backward. It has no counterpart in
+ * the reference. It is for callers that cannot allocate device memory: an
+ * engine that hands out all device memory from its own pool, or a process
+ * that must not grow its device footprint after start-up. points, dL_dd and
+ * dtheta must be device memory of the context's GPU (host buffers are
+ * rejected with UP_ERR_INVALID_ARGUMENT: staging them would need an
+ * allocation). The only scratch is a static device array of 2048 x 43 floats
+ * (352 KiB) that every GPU that loads the library keeps until the process
+ * exits; the kernel never launches more than 2048 blocks, so any point count
+ * fits, and a parameter vector longer than 43 entries is rejected. The first
+ * call on each device looks up the array's device address, so make that
+ * first call before any stream capture begins. All calls share the array:
+ * calls that overlap on the GPU race. */
+int up_sdf_param_backward_noalloc(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta);
+
 /* ---------------------------------------------------------------- batching */
 /* One chunk of a batched run: a synthetic program (per planet), a grid
  * (chunk box and resolution), and output offsets. */

@@ -121,6 +121,7 @@ SIGNATURES = [
     ("up_texture", C.c_int, [C.c_void_p, C.c_int, C.POINTER(MeshIn), C.c_uint32, C.c_uint32, C.c_int, C.POINTER(TextureOut)]),
     ("up_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(TileOut)]),
     ("up_sdf_param_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    ("up_sdf_param_backward_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     ("up_batch_run", C.c_int, [C.c_void_p, C.POINTER(SynthProgram), C.c_size_t, C.POINTER(Chunk), C.c_size_t, C.POINTER(BatchOut)]),
 ]
 

@@ -14,6 +14,7 @@
 #include <vector>
 
 namespace up {
+cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, cudaStream_t s);
 int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
 uint32_t instance_seed(uint32_t seed, uint32_t slot);
 cudaError_t launch_modes_grid(const ModesDesc &M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
@@ -431,6 +432,24 @@ int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const 
 		float *part = (float *)buf(ctx, B_PARTIALS, (size_t)nb * 43 * 4);
 		check(launch_synth_bwd(ctx->prog, dp, n, dw, part, nb, dt, ctx->stream), "adjoint kernel");
 		finish_out(ctx, dtheta, dt, nt * 4);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+// Allocation-free adjoint (see include/up_abi.h): device buffers only, no
+// staging, scratch in a static device array of up_sdf.cu.
+int up_sdf_param_backward_noalloc(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta) {
+	if (!ctx || !points || !dL_dd || !dtheta || n == 0) return UP_ERR_INVALID_ARGUMENT;
+	if (!ctx->synthetic) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "the parameter adjoint needs a synthetic context");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		if (!is_device(points) || !is_device(dL_dd) || !is_device(dtheta))
+			return fail(ctx, UP_ERR_INVALID_ARGUMENT,
+				"up_sdf_param_backward_noalloc needs device buffers: it allocates nothing, so it cannot stage host memory");
+		if (up_synth_theta_count(&ctx->prog) > 43)
+			return fail(ctx, UP_ERR_INVALID_ARGUMENT, "parameter vector longer than the 43-entry scratch row");
+		check(launch_synth_bwd_noalloc(ctx->prog, points, n, dL_dd, dtheta, ctx->stream), "adjoint kernel (no allocation)");
 		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
 		return (int)UP_OK;
 	});

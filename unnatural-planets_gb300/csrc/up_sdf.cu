@@ -10,6 +10,8 @@
 #include "up_internal.h"
 #include "up_synth.cuh"
 
+#include <mutex>
+
 namespace up {
 
 GridDev make_grid(const up_grid &g) {
@@ -185,6 +187,58 @@ cudaError_t launch_synth_bwd(const up_synth_program &P, const float *xyz, uint64
 	m.n = theta_slots(P, m.slot);
 	synth_bwd_reduce<<<1, 64, 0, s>>>(partials, nblocks, m, dtheta);
 	return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- adjoint without allocation
+// Variant of the parameter adjoint for callers that cannot allocate device
+// memory: an engine that hands out all device memory from its own pool, or a
+// host process that must not grow its device footprint after start-up (a
+// fixed budget shared with a renderer or another engine). Its only scratch -- one row of ACC_N partial sums per block -- is
+// this file-scope device array, which every GPU that loads the library keeps
+// until the process exits. The kernel launches at most NOALLOC_MAX_BLOCKS
+// blocks (grid-stride loop), so every point count fits; the array is shared by
+// every call, and each launched block overwrites its whole row before the
+// reduction reads it, so nothing needs clearing. Calls that overlap on the GPU
+// (different streams or host threads) race on the array.
+constexpr int NOALLOC_MAX_BLOCKS = 2048;
+static __device__ __align__(256) float g_noalloc_partials[NOALLOC_MAX_BLOCKS * ACC_N];
+static const size_t NOALLOC_SCRATCH_BYTES = sizeof(float) * NOALLOC_MAX_BLOCKS * ACC_N;
+
+// Host code cannot pass g_noalloc_partials itself: in host code the name is a
+// host-side stand-in, not a device address. The device address is looked up
+// by the first call on each device (with that device current) and cached;
+// that first call should therefore come before any stream capture begins.
+static float *noalloc_scratch(int device, cudaError_t &err) {
+	constexpr int MAX_DEVICES = 64;
+	static std::mutex mu;
+	static float *addr[MAX_DEVICES] = {};
+	err = cudaSuccess;
+	if (device < 0 || device >= MAX_DEVICES) {
+		err = cudaErrorInvalidDevice;
+		return nullptr;
+	}
+	std::lock_guard<std::mutex> lock(mu);
+	if (!addr[device]) {
+		void *p = nullptr;
+		err = cudaGetSymbolAddress(&p, g_noalloc_partials);
+		if (err != cudaSuccess) return nullptr;
+		addr[device] = (float *)p;
+	}
+	return addr[device];
+}
+
+size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_BYTES; }
+int noalloc_max_blocks() { return NOALLOC_MAX_BLOCKS; }
+
+cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, cudaStream_t s) {
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	float *partials = noalloc_scratch(dev, e);
+	if (!partials) return e;
+	int nblocks = synth_bwd_blocks(n);
+	if (nblocks > NOALLOC_MAX_BLOCKS) nblocks = NOALLOC_MAX_BLOCKS;
+	return launch_synth_bwd(P, xyz, n, w, partials, nblocks, dtheta, s);
 }
 
 } // namespace up
