@@ -289,6 +289,8 @@ typedef struct up_batch_out {
 	uint64_t *chunk_vertex_offset; /* nchunks + 1 entries, out (host) */
 	uint64_t *chunk_index_offset;  /* nchunks + 1 entries, out (host) */
 	uint64_t vertex_count, index_count; /* out */
+	float *values;        /* optional: the sampled grids of all chunks, concatenated (x-fastest per chunk) */
+	uint64_t values_capacity;
 } up_batch_out;
 /* Samples and contours many chunks of uneven size (from many planets) in one
  * pass per stage, each stage one launch over all chunks, replayed as a CUDA

@@ -54,6 +54,14 @@ def lib(fast: bool = False) -> C.CDLL:
         "orc_mesh_counts": (None, [vp, vp]),
         "orc_mesh_copy": (None, [vp, vp, vp, vp, vp, vp]),
         "orc_mesh_free": (None, [vp]),
+        "orc_planet_create": (vp, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_uint32, C.c_char_p, C.c_int]),
+        "orc_planet_free": (None, [vp]),
+        "orc_planet_shape": (C.c_int, [vp]),
+        "orc_field_points": (None, [vp, C.c_int, vp, C.c_uint64, C.c_int, vp, vp, C.c_int]),
+        "orc_contour_planet": (vp, [vp, C.c_int, G, vp]),
+        "orc_tiles": (None, [vp, C.c_int, vp, vp, C.c_uint64, vp, vp, C.c_int]),
+        "orc_texture": (None, [vp, C.POINTER(abi.SynthProgram), C.c_int, vp, vp, vp, vp, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int,
+                               vp, vp, vp, vp, vp, vp, vp, C.c_int]),
     }
     for n, (res, args) in sigs.items():
         f = getattr(L, n)
@@ -137,7 +145,50 @@ def grid_positions(grid) -> np.ndarray:
 
 def contour_synth(P, grid, values: np.ndarray) -> dict:
     values = np.ascontiguousarray(values, np.float32)
-    h = lib().orc_contour_synth(C.byref(P), C.byref(grid), _p(values))
+    return _mesh(lib().orc_contour_synth(C.byref(P), C.byref(grid), _p(values)))
+
+
+class Planet:
+    """Oracle planet of the reference modes (shape, elevation, coloring names)."""
+
+    def __init__(self, shape, elevation, coloring="default", poles=False, flowers=False, seed=0):
+        err = C.create_string_buffer(256)
+        self.h = lib().orc_planet_create(shape.encode(), elevation.encode(), coloring.encode(), int(poles), int(flowers), seed, err, 256)
+        if not self.h:
+            raise ValueError(err.value.decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_planet_free(self.h)
+            self.h = None
+
+    @property
+    def shape_index(self) -> int:
+        return lib().orc_planet_shape(self.h)
+
+    def field(self, field, xyz, precision=0, grad=False, threads=8):
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        n = xyz.shape[0]
+        out = np.empty(n, np.float64)
+        g = np.empty((n, 3), np.float64) if grad else None
+        lib().orc_field_points(self.h, field, _p(xyz), n, precision, _p(out), _p(g), threads)
+        return (out, g) if grad else out
+
+    def contour(self, field, grid, values):
+        values = np.ascontiguousarray(values, np.float32)
+        return _mesh(lib().orc_contour_planet(self.h, field, C.byref(grid), _p(values)))
+
+    def tiles(self, purpose, pos, nrm, threads=8):
+        pos = np.ascontiguousarray(pos, np.float32)
+        nrm = np.ascontiguousarray(nrm, np.float32)
+        n = pos.shape[0]
+        out = np.empty((n, 11), np.float64)
+        bt = np.empty((n, 2), np.int32)
+        lib().orc_tiles(self.h, purpose, _p(pos), _p(nrm), n, _p(out), _p(bt), threads)
+        return out, bt
+
+
+def _mesh(h) -> dict:
     try:
         c = np.zeros(4, np.uint64)
         lib().orc_mesh_counts(h, _p(c))
@@ -148,3 +199,18 @@ def contour_synth(P, grid, values: np.ndarray) -> dict:
         return r
     finally:
         lib().orc_mesh_free(h)
+
+
+def texture(purpose, pos, nrm, uv, idx, W, H, dilation=7, planet=None, program=None, threads=8) -> dict:
+    """Texel images of a mesh: float images (NaN where uncovered), 8-bit images
+    and the owning triangle per texel (-1 uncovered)."""
+    pos, nrm = np.ascontiguousarray(pos, np.float32), np.ascontiguousarray(nrm, np.float32)
+    uv, idx = np.ascontiguousarray(uv, np.float32), np.ascontiguousarray(idx, np.uint32)
+    ach = 4 if purpose == 2 else 3
+    r = dict(albedo_f=np.empty((H, W, ach), np.float32), special_f=np.empty((H, W, 2), np.float32), height_f=np.empty((H, W), np.float32),
+             albedo=np.empty((H, W, ach), np.uint8), special=np.empty((H, W, 2), np.uint8), height=np.empty((H, W), np.uint8),
+             owner=np.empty((H, W), np.int32))
+    lib().orc_texture(planet.h if planet is not None else None, C.byref(program) if program is not None else None, purpose, _p(pos),
+                      _p(nrm), _p(uv), _p(idx), idx.shape[0], W, H, dilation, _p(r["albedo_f"]), _p(r["special_f"]),
+                      _p(r["height_f"]), _p(r["albedo"]), _p(r["special"]), _p(r["height"]), _p(r["owner"]), threads)
+    return r

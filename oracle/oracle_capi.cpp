@@ -5,8 +5,10 @@
 #include "oracle_synth.hpp"
 #include "oracle_contour.hpp"
 #include "oracle_modes.hpp"
+#include "oracle_coloring.hpp"
 
 #include <atomic>
+#include <cstdio>
 #include <memory>
 #include <thread>
 #include <vector>
@@ -256,5 +258,119 @@ void orc_mesh_copy(void *h, uint64_t *cells, float *positions, float *normals, u
 	cp(m->r.cells, cells); cp(m->r.positions, positions); cp(m->r.normals, normals); cp(m->r.indices, indices); cp(m->r.edges, edges);
 }
 void orc_mesh_free(void *h) { delete (OrcMesh *)h; }
+
+
+// ---------------------------------------------------------------- reference modes
+void *orc_planet_create(const char *shape, const char *elevation, const char *coloring, int poles, int flowers, uint32_t seed, char *err, int errn) {
+	auto *P = new Planet();
+	const std::string e = make_planet(shape, elevation, coloring, poles != 0, flowers != 0, seed, *P);
+	if (!e.empty()) {
+		if (err && errn > 0) std::snprintf(err, errn, "%s", e.c_str());
+		delete P;
+		return nullptr;
+	}
+	return P;
+}
+void orc_planet_free(void *p) { delete (Planet *)p; }
+int orc_planet_shape(void *p) { return ((Planet *)p)->shape; }
+
+// field values at n points; precision 0 = FP64, 1 = FP32; grad (FP64 dual) when not null
+void orc_field_points(void *h, int field, const float *xyz, uint64_t n, int precision, double *out, double *grad, int threads) {
+	const Planet &P = *(Planet *)h;
+	parallel_for(n, threads, [&](uint64_t i) {
+		const float *q = xyz + 3 * i;
+		if (grad) {
+			V3<Dual<3>> p(Dual<3>::var(q[0], 0), Dual<3>::var(q[1], 1), Dual<3>::var(q[2], 2));
+			const Dual<3> v = field_eval(P, field, p);
+			out[i] = v.v;
+			for (int a = 0; a < 3; a++) grad[3 * i + a] = v.d[a];
+		} else if (precision == 1) {
+			out[i] = val(field_eval(P, field, V3<F32>(q[0], q[1], q[2])));
+		} else {
+			out[i] = field_eval(P, field, V3<double>(q[0], q[1], q[2]));
+		}
+	});
+}
+
+static GradFn planet_gradfn(const Planet *P, int field) {
+	return [P, field](const double p[3], double g[3]) {
+		V3<Dual<3>> q(Dual<3>::var(p[0], 0), Dual<3>::var(p[1], 1), Dual<3>::var(p[2], 2));
+		const Dual<3> v = field_eval(*P, field, q);
+		for (int a = 0; a < 3; a++) g[a] = v.d[a];
+	};
+}
+void *orc_contour_planet(void *h, int field, const up_grid *grid, const float *values) {
+	auto *m = new OrcMesh();
+	contour(*grid, values, planet_gradfn((Planet *)h, field), m->r);
+	return m;
+}
+
+// per-point tiles: 11 floats per point out (albedo rgb, roughness, metallic,
+// height, opacity, elevation, slope, temperature, precipitation) + biome, type
+void orc_tiles(void *h, int purpose, const float *pos, const float *nrm, uint64_t n, double *out11, int32_t *biome_type, int threads) {
+	const Planet &P = *(Planet *)h;
+	Col<double> col(P);
+	parallel_for(n, threads, [&](uint64_t i) {
+		Tile<double> t;
+		t.position = V3<double>(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+		t.normal = V3<double>(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+		t.purpose = purpose;
+		col.run(t);
+		double *o = out11 + 11 * i;
+		o[0] = t.albedo.x; o[1] = t.albedo.y; o[2] = t.albedo.z; o[3] = t.roughness; o[4] = t.metallic; o[5] = t.height; o[6] = t.opacity;
+		o[7] = t.elevation; o[8] = t.slope; o[9] = t.temperature; o[10] = t.precipitation;
+		biome_type[2 * i] = t.biome;
+		biome_type[2 * i + 1] = t.type;
+	});
+}
+
+// texels: rasterise, color (planet or synthetic program), optional dilation,
+// float images (NaN where uncovered) and 8-bit images. purpose 1 land (RGB),
+// 2 water (RGBA). Either planet or prog is not null.
+void orc_texture(void *planet, const up_synth_program *prog, int purpose, const float *pos, const float *nrm, const float *uv,
+	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, float *albedo_f, float *special_f, float *height_f,
+	uint8_t *albedo8, uint8_t *special8, uint8_t *height8, int32_t *owner, int threads) {
+	Raster R;
+	rasterize(uv, idx, nidx / 3, W, H, R);
+	const int ach = purpose == PU_WATER ? 4 : 3;
+	std::vector<float> A((size_t)W * H * ach, NAN), S((size_t)W * H * 2, NAN), Hh((size_t)W * H, NAN);
+	parallel_for((uint64_t)H, threads, [&](uint64_t y) {
+		for (uint32_t x = 0; x < W; x++) {
+			const size_t q = (size_t)y * W + x;
+			const int32_t t = R.owner[q];
+			if (t < 0) continue;
+			V3<double> p, nn;
+			for (int k = 0; k < 3; k++) {
+				const uint32_t v = idx[3 * (uint64_t)t + k];
+				const double w = R.w[3 * q + k];
+				p = p + V3<double>(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]) * w;
+				nn = nn + V3<double>(nrm[3 * v], nrm[3 * v + 1], nrm[3 * v + 2]) * w;
+			}
+			nn = normalize(nn);
+			V3<double> alb;
+			double rough, metal = 0, height, opacity = 1;
+			if (planet) {
+				Tile<double> tl;
+				tl.position = p; tl.normal = nn; tl.purpose = purpose;
+				Col<double>(*(Planet *)planet).run(tl);
+				alb = tl.albedo; rough = tl.roughness; metal = tl.metallic; height = tl.height; opacity = tl.opacity;
+			} else {
+				synth_texel(*prog, p, alb, rough, height);
+			}
+			A[q * ach] = (float)alb.x; A[q * ach + 1] = (float)alb.y; A[q * ach + 2] = (float)alb.z;
+			if (ach == 4) A[q * ach + 3] = (float)opacity;
+			S[2 * q] = (float)rough; S[2 * q + 1] = (float)metal;
+			Hh[q] = (float)height;
+		}
+	});
+	if (dilation > 0) { dilate(A, W, H, ach, dilation); dilate(S, W, H, 2, dilation); dilate(Hh, W, H, 1, dilation); }
+	if (albedo_f) std::copy(A.begin(), A.end(), albedo_f);
+	if (special_f) std::copy(S.begin(), S.end(), special_f);
+	if (height_f) std::copy(Hh.begin(), Hh.end(), height_f);
+	for (size_t i = 0; albedo8 && i < A.size(); i++) albedo8[i] = to_u8(A[i]);
+	for (size_t i = 0; special8 && i < S.size(); i++) special8[i] = to_u8(S[i]);
+	for (size_t i = 0; height8 && i < Hh.size(); i++) height8[i] = to_u8(Hh[i]);
+	if (owner) std::copy(R.owner.begin(), R.owner.end(), owner);
+}
 
 } // extern "C"

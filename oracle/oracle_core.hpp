@@ -143,12 +143,10 @@ struct V3 {
 template<class T> inline V3<T> operator+(const V3<T> &a, const V3<T> &b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 template<class T> inline V3<T> operator-(const V3<T> &a, const V3<T> &b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 template<class T> inline V3<T> operator-(const V3<T> &a) { return {-a.x, -a.y, -a.z}; }
-template<class T> inline V3<T> operator*(const V3<T> &a, const T &s) { return {a.x * s, a.y * s, a.z * s}; }
-template<class T> inline V3<T> operator*(const T &s, const V3<T> &a) { return a * s; }
-template<class T> inline V3<T> operator*(const V3<T> &a, double s) { return a * T(s); }
+template<class T, class S> inline V3<T> operator*(const V3<T> &a, const S &s) { return {a.x * s, a.y * s, a.z * s}; }
+template<class T, class S> inline V3<T> operator*(const S &s, const V3<T> &a) { return {a.x * s, a.y * s, a.z * s}; }
 template<class T> inline V3<T> operator*(const V3<T> &a, const V3<T> &b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-template<class T> inline V3<T> operator/(const V3<T> &a, const T &s) { return {a.x / s, a.y / s, a.z / s}; }
-template<class T> inline V3<T> operator/(const V3<T> &a, double s) { return a / T(s); }
+template<class T, class S> inline V3<T> operator/(const V3<T> &a, const S &s) { return {a.x / s, a.y / s, a.z / s}; }
 template<class T> inline T dot(const V3<T> &a, const V3<T> &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 template<class T> inline T length(const V3<T> &a) { return sqrt(dot(a, a)); }
 template<class T> inline V3<T> normalize(const V3<T> &a) { return a / length(a); }

@@ -3,6 +3,13 @@
 // GPU. It exercises arithmetic only; the kernels themselves run in the GPU
 // tests. Built by tests/hostcheck/build_hostcheck.py into tests/hostcheck/_build.
 #include "../../unnatural-planets_gb300/csrc/up_synth.cuh"
+#include "../../unnatural-planets_gb300/csrc/up_modes.cuh"
+#include "../../unnatural-planets_gb300/csrc/up_coloring.cuh"
+#include <string>
+
+namespace up {
+int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
+}
 
 using namespace up;
 
@@ -53,5 +60,49 @@ uint32_t hc_lattice_hash(int x, int y, int z, uint32_t key) { return lattice_has
 uint32_t hc_corner_hash(int x, int y, int z, uint32_t key, int b) {
 	Cell c; c.ix = x; c.iy = y; c.iz = z; c.fx = c.fy = c.fz = 0.f;
 	return corner_hashes(c, key).h[b];
+}
+
+// reference-mode planet built by the product's host builder
+void *hc_modes_create(const char *shape, const char *elevation, const char *coloring, int poles, int flowers, uint32_t seed) {
+	up_modes m{shape, elevation, coloring, poles, flowers};
+	auto *D = new ModesDesc();
+	std::string name, err;
+	bool ds;
+	if (build_modes(m, seed, *D, name, ds, err) != UP_OK) { delete D; return nullptr; }
+	return D;
+}
+void hc_modes_free(void *d) { delete (ModesDesc *)d; }
+void hc_modes_field(void *d, int field, const float *xyz, uint64_t n, float *out, float *grad) {
+	const ModesDesc &M = *(ModesDesc *)d;
+	for (uint64_t i = 0; i < n; i++) {
+		const V3f p = v3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+		if (grad) {
+			const Df f = field_eval(M, field, dual_point(p));
+			out[i] = f.v;
+			grad[3 * i] = f.d.x; grad[3 * i + 1] = f.d.y; grad[3 * i + 2] = f.d.z;
+		} else {
+			out[i] = field_eval(M, field, vs(p.x, p.y, p.z));
+		}
+	}
+}
+
+// per-point tiles with the device coloring pipeline (11 floats + biome, type)
+void hc_tiles(void *d, int purpose, const float *pos, const float *nrm, uint64_t n, float *out11, int32_t *bt) {
+	const ModesDesc &M = *(ModesDesc *)d;
+	for (uint64_t i = 0; i < n; i++) {
+		TileD t = tile_init(v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), v3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]), purpose);
+		color_tile(M, t);
+		float *o = out11 + 11 * i;
+		o[0] = t.albedo.x; o[1] = t.albedo.y; o[2] = t.albedo.z; o[3] = t.roughness; o[4] = t.metallic; o[5] = t.height; o[6] = t.opacity;
+		o[7] = t.elevation; o[8] = t.slope; o[9] = t.temperature; o[10] = t.precipitation;
+		bt[2 * i] = t.biome; bt[2 * i + 1] = t.type;
+	}
+}
+void hc_synth_texel(const up_synth_program *P, const float *pos, uint64_t n, float *out5) {
+	for (uint64_t i = 0; i < n; i++) {
+		V3f a; float r, h;
+		synth_texel(*P, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), a, r, h);
+		out5[5 * i] = a.x; out5[5 * i + 1] = a.y; out5[5 * i + 2] = a.z; out5[5 * i + 3] = r; out5[5 * i + 4] = h;
+	}
 }
 }

@@ -1,0 +1,56 @@
+"""torch.autograd wrapper over the C-ABI adjoint: gradients against the
+oracle's FP64 forward-mode theta gradient, and a short inverse fit (the
+benchmark's differentiation workload, scaled down) that recovers a perturbed
+parameter vector."""
+from __future__ import annotations
+
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def test_backward_matches_oracle(cuda, up, O):
+    torch = cuda
+    AG = importlib.import_module("unnatural-planets_gb300.autograd")
+    W = workloads()
+    P = W.torus_spheres_ridged_cellular()
+    planet = up.Planet(program=P)
+    x = np.random.default_rng(2).uniform(-1.4, 1.4, size=(40000, 3)).astype(np.float32)
+    pts = torch.from_numpy(x).cuda()
+    theta = torch.from_numpy(W.theta_of(P)).cuda().requires_grad_(True)
+    d = AG.sdf(theta, pts, planet)
+    loss = (d * d).mean()
+    loss.backward()
+    w = 2.0 * d.detach().cpu().numpy().astype(np.float64) / len(x)
+    ref = O.synth_theta_grad(P, x, w)
+    got = theta.grad.cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-3 * np.abs(ref).max()
+
+
+def test_inverse_fit_recovers_parameters(cuda, up):
+    torch = cuda
+    AG = importlib.import_module("unnatural-planets_gb300.autograd")
+    W = workloads()
+    target = W.sphere_fbm(seed=5)
+    t_star = torch.from_numpy(W.theta_of(target)).cuda()
+    x = torch.from_numpy(W.shell_points(1.0, 0.1, 200000, seed=9)).cuda()
+    planet_t = up.Planet(program=target)
+    d_star = planet_t.sdf_points(x, d=torch.empty(x.shape[0], device="cuda"))
+    rng = np.random.default_rng(6)
+    t0 = t_star.cpu().numpy() * (1 + 0.15 * rng.uniform(-1, 1, size=t_star.shape[0])).astype(np.float32)
+    theta = torch.tensor(t0, device="cuda", requires_grad=True)
+    planet = up.Planet(program=W.sphere_fbm(seed=5))
+    opt = torch.optim.Adam([theta], lr=1e-2)
+    first = None
+    for _ in range(150):
+        opt.zero_grad()
+        loss = ((AG.sdf(theta, x, planet) - d_star) ** 2).mean()
+        loss.backward()
+        opt.step()
+        first = first if first is not None else float(loss.detach())
+    assert float(loss.detach()) < 0.05 * first

@@ -121,3 +121,77 @@ class Planet:
             dtheta = np.empty(nt, np.float32)
         self._check(self.lib.up_sdf_param_backward(self.h, _addr(xyz), n, _addr(dL_dd), _addr(dtheta)))
         return dtheta
+
+    # ---- texels
+    def texture(self, purpose, pos, nrm, uv, idx, width, height, dilation=7, floats=False):
+        """Texel images of an unwrapped mesh (numpy host buffers or torch
+        device tensors). Returns a dict of numpy arrays: albedo (H, W, 3|4),
+        special (H, W, 2), height (H, W) as uint8, and the float images when
+        floats=True."""
+        ach = 4 if purpose == abi.PURPOSE_WATER else 3
+        n = width * height
+        res = dict(albedo=np.empty((height, width, ach), np.uint8), special=np.empty((height, width, 2), np.uint8),
+                   height=np.empty((height, width), np.uint8))
+        if floats:
+            res.update(albedo_f=np.empty((height, width, ach), np.float32), special_f=np.empty((height, width, 2), np.float32),
+                       height_f=np.empty((height, width), np.float32))
+        m = abi.MeshIn(_addr(pos), _addr(nrm), _addr(uv), _addr(idx), int(pos.shape[0]), int(idx.shape[0]))
+        o = abi.TextureOut(_addr(res["albedo"]), _addr(res["special"]), _addr(res["height"]), _addr(res.get("albedo_f")),
+                           _addr(res.get("special_f")), _addr(res.get("height_f")))
+        self._check(self.lib.up_texture(self.h, purpose, C.byref(m), width, height, dilation, C.byref(o)))
+        del n
+        return res
+
+    def tiles(self, purpose, pos, nrm):
+        """terrainTile for n points: (floats (n, 11): albedo rgb, roughness,
+        metallic, height, opacity, elevation, slope, temperature,
+        precipitation; uint8 (n, 2): biome, type)."""
+        n = int(pos.shape[0])
+        f = {k: np.empty(n, np.float32) for k in ("roughness", "metallic", "height", "opacity", "elevation", "slope", "temperature",
+                                                    "precipitation")}
+        alb = np.empty((n, 3), np.float32)
+        bio = np.empty(n, np.uint8)
+        typ = np.empty(n, np.uint8)
+        o = abi.TileOut(_addr(alb), _addr(f["roughness"]), _addr(f["metallic"]), _addr(f["height"]), _addr(f["opacity"]),
+                        _addr(f["elevation"]), _addr(f["slope"]), _addr(f["temperature"]), _addr(f["precipitation"]), _addr(bio),
+                        _addr(typ))
+        self._check(self.lib.up_tiles(self.h, purpose, _addr(pos), _addr(nrm), n, C.byref(o)))
+        out = np.concatenate([alb, np.stack([f[k] for k in ("roughness", "metallic", "height", "opacity", "elevation", "slope",
+                                                            "temperature", "precipitation")], axis=1)], axis=1)
+        return out, np.stack([bio, typ], axis=1)
+
+
+def batch_run(planet_or_lib, planets, chunks, values=False, device=False):
+    """Sample and contour many chunks (up_batch_run). `planet_or_lib` is any
+    Planet (its context runs the batch). Returns dict with positions (V,3),
+    indices (I,), per-chunk vertex/index offsets (n+1,) and optionally the
+    concatenated sampled values."""
+    ctx = planet_or_lib
+    P = (abi.SynthProgram * len(planets))(*planets)
+    Cs = (abi.Chunk * len(chunks))(*[abi.Chunk(p, g) for p, g in chunks])
+    vo = np.zeros(len(chunks) + 1, np.uint64)
+    io = np.zeros(len(chunks) + 1, np.uint64)
+    o = abi.BatchOut(None, None, 0, 0, vo.ctypes.data, io.ctypes.data, 0, 0, None, 0)
+    st = ctx.lib.up_batch_run(ctx.h, P, len(planets), Cs, len(chunks), C.byref(o))
+    if st != abi.UP_ERR_CAPACITY:
+        ctx._check(st)
+    V, I = int(o.vertex_count), int(o.index_count)
+    nval = sum(g.count for _, g in chunks)
+    if device:
+        import torch
+        pos = torch.empty((V, 3), device="cuda")
+        idx = torch.empty(I, dtype=torch.int32, device="cuda")
+        val = torch.empty(nval, device="cuda") if values else None
+    else:
+        pos = np.empty((V, 3), np.float32)
+        idx = np.empty(I, np.uint32)
+        val = np.empty(nval, np.float32) if values else None
+    o = abi.BatchOut(_addr(pos), _addr(idx), V, I, vo.ctypes.data, io.ctypes.data, 0, 0, _addr(val), nval if values else 0)
+    ctx._check(ctx.lib.up_batch_run(ctx.h, P, len(planets), Cs, len(chunks), C.byref(o)))
+    return dict(positions=pos, indices=idx, vertex_offsets=vo.copy(), index_offsets=io.copy(), values=val, _args=(P, Cs, o))
+
+
+def batch_replay(ctx, prepared):
+    """Run the same batch again (graph replay inside the library)."""
+    P, Cs, o = prepared["_args"]
+    ctx._check(ctx.lib.up_batch_run(ctx.h, P, len(P), Cs, len(Cs), C.byref(o)))

@@ -95,7 +95,7 @@ class Chunk(C.Structure):
 class BatchOut(C.Structure):
     _fields_ = [("positions", C.c_void_p), ("indices", C.c_void_p), ("vertex_capacity", C.c_uint64),
                 ("index_capacity", C.c_uint64), ("chunk_vertex_offset", C.c_void_p), ("chunk_index_offset", C.c_void_p),
-                ("vertex_count", C.c_uint64), ("index_count", C.c_uint64)]
+                ("vertex_count", C.c_uint64), ("index_count", C.c_uint64), ("values", C.c_void_p), ("values_capacity", C.c_uint64)]
 
 
 # (name, restype, argtypes) of every entry point in include/up_abi.h

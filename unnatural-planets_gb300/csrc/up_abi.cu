@@ -17,10 +17,18 @@ namespace up {
 cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, cudaStream_t s);
 int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
 uint32_t instance_seed(uint32_t seed, uint32_t slot);
-cudaError_t launch_modes_grid(const ModesDesc &M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
+cudaError_t launch_modes_grid(const ModesDesc *M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
 	unsigned *nanflag, cudaStream_t s);
-cudaError_t launch_modes_points(const ModesDesc &M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag,
+cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag,
 	cudaStream_t s);
+cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int purpose, const float *pos, const float *nrm, const float *uv,
+	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, int *owner, float *img0, float *img1, uint8_t *a8, uint8_t *s8,
+	uint8_t *h8, float *af, float *sf, float *hf, int *launches, cudaStream_t s);
+cudaError_t tiles_run(const ModesDesc *M, int purpose, const float *pos, const float *nrm, uint64_t n, float *out11, uint8_t *bt, cudaStream_t s);
+void batch_state_free(void *p);
+cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks,
+	uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
+	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, cudaStream_t caller);
 } // namespace up
 
 using namespace up;
@@ -40,11 +48,13 @@ struct up_context {
 	bool synthetic = false;
 	up_synth_program prog{};
 	ModesDesc modes{};
+	ModesDesc *d_modes = nullptr; // device copy read by the mode kernels
 	std::string shape_name;
 	bool double_sided = false;
 	std::string last_error;
 	unsigned *d_flag = nullptr;
 	struct Buf { void *p = nullptr; size_t n = 0; } bufs[B_COUNT];
+	void *batch = nullptr; // planned batch (up_batch.cu)
 };
 
 namespace {
@@ -222,8 +232,16 @@ int up_context_create(const up_modes *modes, const up_seeds *seeds, up_context *
 		delete ctx;
 		return st;
 	}
-	const int r = guarded(ctx, [&]() { return init_context(ctx); });
+	const int r = guarded(ctx, [&]() {
+		const int st2 = init_context(ctx);
+		if (st2 != UP_OK) return st2;
+		check(cudaMalloc(&ctx->d_modes, sizeof(ModesDesc)), "cudaMalloc planet description");
+		check(cudaMemcpy(ctx->d_modes, &ctx->modes, sizeof(ModesDesc), cudaMemcpyHostToDevice), "cudaMemcpy planet description");
+		return (int)UP_OK;
+	});
 	if (r != UP_OK) {
+		if (ctx->d_modes) cudaFree(ctx->d_modes);
+		if (ctx->d_flag) cudaFree(ctx->d_flag);
 		delete ctx;
 		return r;
 	}
@@ -257,6 +275,8 @@ int up_context_destroy(up_context *ctx) {
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
 	for (auto &b : ctx->bufs) if (b.p) cudaFree(b.p);
 	if (ctx->d_flag) cudaFree(ctx->d_flag);
+	if (ctx->d_modes) cudaFree(ctx->d_modes);
+	if (ctx->batch) batch_state_free(ctx->batch);
 	delete ctx;
 	return UP_OK;
 }
@@ -311,7 +331,7 @@ int up_sdf_eval_points(up_context *ctx, int field, const float *xyz, size_t n, f
 		float *dg = (float *)stage_out(ctx, B_GRAD, grad, n * 12);
 		reset_flag(ctx);
 		if (ctx->synthetic) check(launch_synth_points(ctx->prog, dx, n, dd, dg, ctx->d_flag, ctx->stream), "sdf points kernel");
-		else check(launch_modes_points(ctx->modes, field, dx, n, dd, dg, ctx->d_flag, ctx->stream), "sdf points kernel");
+		else check(launch_modes_points(ctx->d_modes, field, dx, n, dd, dg, ctx->d_flag, ctx->stream), "sdf points kernel");
 		finish_out(ctx, d, dd, n * 4);
 		finish_out(ctx, grad, dg, n * 12);
 		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
@@ -347,7 +367,7 @@ int up_sdf_grid(up_context *ctx, uint32_t mask, const up_grid *grid, float *cons
 		float *dg = (float *)stage_out(ctx, B_GRAD, grad, n * 12);
 		reset_flag(ctx);
 		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, g, o[0], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
-		else check(launch_modes_grid(ctx->modes, mask, g, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		else check(launch_modes_grid(ctx->d_modes, mask, g, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
 		for (int f = 0; f < 3; f++)
 			if (mask >> f & 1u) finish_out(ctx, out[f], o[f], n * 4);
 		finish_out(ctx, grad, dg, n * 12);
@@ -379,7 +399,7 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 			else {
 				float *o[3] = {nullptr, nullptr, nullptr};
 				o[field] = gd;
-				check(launch_modes_grid(ctx->modes, 1u << field, g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+				check(launch_modes_grid(ctx->d_modes, 1u << field, g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
 			}
 			if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
 			d = gd;
@@ -410,7 +430,7 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 		float *nrm = (float *)stage_out(ctx, B_MESH_NRM, mesh->normals, (size_t)ncells * 12);
 		uint32_t *idx = (uint32_t *)stage_out(ctx, B_MESH_IDX, mesh->indices, (size_t)nquads * 24);
 		if (ctx->synthetic) check(dc_geometry_synth(ctx->prog, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
-		else check(dc_geometry_modes(ctx->modes, field, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
+		else check(dc_geometry_modes(ctx->d_modes, field, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
 		finish_out(ctx, mesh->positions, pos, (size_t)ncells * 12);
 		finish_out(ctx, mesh->normals, nrm, (size_t)ncells * 12);
 		finish_out(ctx, mesh->indices, idx, (size_t)nquads * 24);
@@ -450,6 +470,107 @@ int up_sdf_param_backward_noalloc(up_context *ctx, const float *points, size_t n
 		if (up_synth_theta_count(&ctx->prog) > 43)
 			return fail(ctx, UP_ERR_INVALID_ARGUMENT, "parameter vector longer than the 43-entry scratch row");
 		check(launch_synth_bwd_noalloc(ctx->prog, points, n, dL_dd, dtheta, ctx->stream), "adjoint kernel (no allocation)");
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_texture(up_context *ctx, int purpose, const up_mesh_in *mesh, uint32_t width, uint32_t height, int dilation, up_texture_out *out) {
+	if (!ctx || !mesh || !out || width == 0 || height == 0 || dilation < 0) return UP_ERR_INVALID_ARGUMENT;
+	if (purpose != UP_PURPOSE_LAND && purpose != UP_PURPOSE_WATER) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "purpose must be LAND or WATER");
+	if (!mesh->positions || !mesh->normals || !mesh->uvs || !mesh->indices || mesh->index_count % 3 != 0)
+		return fail(ctx, UP_ERR_INVALID_ARGUMENT, "mesh needs positions, normals, uvs and a multiple of 3 indices");
+	if ((uint64_t)width * height >= (1ull << 31)) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "atlas too large");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const uint64_t V = mesh->vertex_count, I = mesh->index_count, n = (uint64_t)width * height;
+		const int ach = purpose == UP_PURPOSE_WATER ? 4 : 3;
+		const float *pos = (const float *)stage_in(ctx, B_TEX0, mesh->positions, V * 12);
+		const float *nrm = (const float *)stage_in(ctx, B_TEX1, mesh->normals, V * 12);
+		const float *uv = (const float *)stage_in(ctx, B_TEX2, mesh->uvs, V * 8);
+		const uint32_t *idx = (const uint32_t *)stage_in(ctx, B_TEX3, mesh->indices, I * 4);
+		int *owner = (int *)buf(ctx, B_TEX4, n * 4);
+		float *img0 = (float *)buf(ctx, B_TEX5, n * (ach + 3) * 4);
+		float *img1 = dilation > 0 ? (float *)buf(ctx, B_TEX6, n * (ach + 3) * 4) : nullptr;
+		uint8_t *a8 = (uint8_t *)stage_out(ctx, B_TEX7, out->albedo, n * ach);
+		uint8_t *s8 = (uint8_t *)stage_out(ctx, B_TEX8, out->special, n * 2);
+		uint8_t *h8 = (uint8_t *)stage_out(ctx, B_TEX9, out->height, n);
+		float *af = (float *)stage_out(ctx, B_BATCH0, out->albedo_f32, n * ach * 4);
+		float *sf = (float *)stage_out(ctx, B_BATCH1, out->special_f32, n * 8);
+		float *hf = (float *)stage_out(ctx, B_BATCH2, out->height_f32, n * 4);
+		check(texture_run(ctx->synthetic ? nullptr : ctx->d_modes, ctx->synthetic ? &ctx->prog : nullptr, purpose, pos, nrm, uv, idx, I,
+			width, height, dilation, owner, img0, img1, a8, s8, h8, af, sf, hf, nullptr, ctx->stream), "texture kernels");
+		finish_out(ctx, out->albedo, a8, n * ach);
+		finish_out(ctx, out->special, s8, n * 2);
+		finish_out(ctx, out->height, h8, n);
+		finish_out(ctx, out->albedo_f32, af, n * ach * 4);
+		finish_out(ctx, out->special_f32, sf, n * 8);
+		finish_out(ctx, out->height_f32, hf, n * 4);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_tiles(up_context *ctx, int purpose, const float *positions, const float *normals, size_t n, up_tile_out *out) {
+	if (!ctx || !positions || !normals || !out || n == 0) return UP_ERR_INVALID_ARGUMENT;
+	if (ctx->synthetic) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "tiles need a reference-mode context");
+	if (purpose < UP_PURPOSE_LAND || purpose > UP_PURPOSE_NAVIGATION) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "bad purpose");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const float *p = (const float *)stage_in(ctx, B_IN0, positions, n * 12);
+		const float *q = (const float *)stage_in(ctx, B_GRAD, normals, n * 12);
+		float *o11 = (float *)buf(ctx, B_OUT0, n * 44);
+		uint8_t *bt = (uint8_t *)buf(ctx, B_OUT1, n * 2);
+		check(tiles_run(ctx->d_modes, purpose, p, q, n, o11, bt, ctx->stream), "tiles kernel");
+		// one plane per field; destinations may be host or device memory
+		float *dst[9] = {out->roughness, out->metallic, out->height, out->opacity, out->elevation, out->slope, out->temperature,
+			out->precipitation, nullptr};
+		for (int c = 0; out->albedo && c < 3; c++) // plane c -> every third float
+			check(cudaMemcpy2DAsync(out->albedo + c, 3 * sizeof(float), o11 + (size_t)c * n, sizeof(float), sizeof(float), n, cudaMemcpyDefault,
+				ctx->stream), "cudaMemcpy2DAsync albedo");
+		for (int k = 0; k < 8; k++)
+			if (dst[k]) check(cudaMemcpyAsync(dst[k], o11 + (size_t)(3 + k) * n, n * 4, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync tiles");
+		if (out->biome) check(cudaMemcpyAsync(out->biome, bt, n, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync biome");
+		if (out->type) check(cudaMemcpyAsync(out->type, bt + n, n, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync type");
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_batch_run(up_context *ctx, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks, up_batch_out *out) {
+	if (!ctx || !planets || !chunks || !out || nplanets == 0 || nchunks == 0) return UP_ERR_INVALID_ARGUMENT;
+	for (size_t i = 0; i < nplanets; i++)
+		if (!valid_program(planets[i])) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "invalid planet program");
+	for (size_t c = 0; c < nchunks; c++)
+		if (chunks[c].planet >= nplanets || !valid_grid(&chunks[c].grid)) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "invalid chunk");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		uint32_t ncells = 0, nquads = 0;
+		std::vector<uint32_t> cc, cq;
+		const float *dpos = nullptr, *dval = nullptr;
+		const uint32_t *didx = nullptr;
+		uint64_t nval = 0;
+		bool nan = false, replayed = false;
+		check(batch_execute(ctx->batch, planets, nplanets, chunks, nchunks, ncells, nquads, cc, cq, dpos, didx, dval, nval, nan, replayed,
+			ctx->stream), "batch kernels");
+		if (nan) return fail(ctx, UP_ERR_NAN, "invalid land sdf value");
+		out->vertex_count = ncells;
+		out->index_count = 6ull * nquads;
+		if (out->chunk_vertex_offset)
+			for (size_t c = 0; c <= nchunks; c++) out->chunk_vertex_offset[c] = cc[c];
+		if (out->chunk_index_offset)
+			for (size_t c = 0; c <= nchunks; c++) out->chunk_index_offset[c] = 6ull * cq[c];
+		if (!out->positions || !out->indices || out->vertex_capacity < ncells || out->index_capacity < 6ull * nquads)
+			return fail(ctx, UP_ERR_CAPACITY, "batch output buffers too small");
+		if (out->values && out->values_capacity < nval) return fail(ctx, UP_ERR_CAPACITY, "batch values buffer too small");
+		const cudaMemcpyKind kp = is_device(out->positions) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+		check(cudaMemcpyAsync(out->positions, dpos, (size_t)ncells * 12, kp, ctx->stream), "cudaMemcpyAsync batch positions");
+		const cudaMemcpyKind ki = is_device(out->indices) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+		check(cudaMemcpyAsync(out->indices, didx, (size_t)nquads * 24, ki, ctx->stream), "cudaMemcpyAsync batch indices");
+		if (out->values) {
+			const cudaMemcpyKind kv = is_device(out->values) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+			check(cudaMemcpyAsync(out->values, dval, (size_t)nval * 4, kv, ctx->stream), "cudaMemcpyAsync batch values");
+		}
 		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
 		return (int)UP_OK;
 	});

@@ -1,0 +1,435 @@
+// Batched sampling and dual contouring of many chunks of uneven size, from
+// many planets, with one launch per stage over all chunks.
+//
+// No direct reference counterpart: the reference contours one planet field
+// at a time (sources/meshGeneration.cpp:32-44) and fans chunk work out over
+// CPU tasks (tasksRunBlocking, sources/generator.cpp:159,215).
+//
+// Stages (each one launch covering every chunk):
+//   sample  persistent blocks pull 1024-sample tiles from a device work
+//           counter; a tile belongs to one chunk (binary search of the tile
+//           table); values go to one concatenated grid
+//   count   per 1024-point block of every chunk: active cells, sign edges,
+//           quads (same rules as up_contour.cuh)
+//   scan    exclusive scan of all block counts (global order = chunk order)
+//   offsets per-chunk list offsets from the scan
+//   emit    ordered lists and per-chunk maps
+//   hermite / qef / quads  over the global lists, chunk found by binary search
+// The first call for a given (planets, chunks) input runs eagerly (the host
+// needs the totals to size the lists), autotunes the sampling block size
+// among 128/256/512 threads, then captures the stages in a CUDA graph on a
+// private stream; later calls with byte-identical inputs replay the graph
+// (the same work, recomputed) without host round trips.
+#include "up_contour.cuh"
+#include "up_synth.cuh"
+
+#include <cstring>
+#include <vector>
+
+namespace up {
+
+struct BatchChunkDev {
+	GridDev g;
+	uint32_t planet;
+	uint32_t pt_off, cell_off, blk_off, tile_off;
+};
+
+constexpr uint32_t BATCH_TILE = 1024;
+
+__device__ __forceinline__ uint32_t find_chunk(const uint32_t *__restrict__ starts, uint32_t n, uint32_t x) {
+	// last c with starts[c] <= x (starts ascending, starts[0] = 0)
+	uint32_t lo = 0, hi = n;
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (starts[mid] <= x) lo = mid;
+		else hi = mid;
+	}
+	return lo;
+}
+
+__device__ __forceinline__ float bgrid_coord(const GridDev &g, int a, uint32_t i) {
+	return __fadd_rn(__fmul_rn((float)i, g.step[a]), g.lo[a]);
+}
+
+template<int THREADS>
+__global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ tile_starts, uint32_t nchunks, uint32_t ntiles, float *__restrict__ d, unsigned *__restrict__ counter,
+	unsigned *__restrict__ nanflag) {
+	__shared__ uint32_t tile;
+	bool bad = false;
+	for (;;) {
+		if (threadIdx.x == 0) tile = atomicAdd(counter, 1u);
+		__syncthreads();
+		const uint32_t t = tile;
+		__syncthreads();
+		if (t >= ntiles) break;
+		const uint32_t c = find_chunk(tile_starts, nchunks, t);
+		const BatchChunkDev &ch = chunks[c];
+		const up_synth_program &P = planets[ch.planet];
+		const uint32_t nx = ch.g.n[0], ny = ch.g.n[1];
+		const uint32_t npts = nx * ny * ch.g.n[2];
+		const uint32_t base = (t - ch.tile_off) * BATCH_TILE;
+		#pragma unroll 1
+		for (uint32_t it = threadIdx.x; it < BATCH_TILE; it += THREADS) {
+			const uint32_t s = base + it;
+			if (s >= npts) break;
+			const uint32_t i = s % nx, r = s / nx, j = r % ny, k = r / ny;
+			const float v = synth_eval<false, -1, -1>(P, v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k))).v;
+			d[ch.pt_off + s] = v;
+			bad |= isnan(v);
+		}
+	}
+	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
+}
+
+__global__ void __launch_bounds__(DC_T) batch_count_kernel(const float *__restrict__ d, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ blk_starts, uint32_t nchunks, uint32_t nblocks, uint32_t *__restrict__ blk) {
+	const uint32_t c = find_chunk(blk_starts, nchunks, blockIdx.x);
+	const BatchChunkDev &ch = chunks[c];
+	const uint32_t npts = ch.g.n[0] * ch.g.n[1] * ch.g.n[2];
+	const uint32_t base = (blockIdx.x - ch.blk_off) * DC_PB + threadIdx.x * DC_ITEMS;
+	const float *dc = d + ch.pt_off;
+	uint64_t cnt = 0;
+	#pragma unroll
+	for (int it = 0; it < DC_ITEMS; it++) {
+		const uint32_t p = base + it;
+		if (p < npts) cnt += pack_counts(point_flags(dc, ch.g, p));
+	}
+	uint64_t tot;
+	block_exscan<DC_T>(cnt, tot);
+	if (threadIdx.x == 0) {
+		blk[blockIdx.x] = (uint32_t)(tot & 0x1FFFFF);
+		blk[nblocks + blockIdx.x] = (uint32_t)((tot >> 21) & 0x1FFFFF);
+		blk[2 * nblocks + blockIdx.x] = (uint32_t)(tot >> 42);
+	}
+}
+
+// per-chunk offsets of the three lists (+ totals at index nchunks)
+__global__ void batch_offsets_kernel(const BatchChunkDev *__restrict__ chunks, uint32_t nchunks, uint32_t nblocks, const uint32_t *__restrict__ blk,
+	const uint32_t *__restrict__ totals, uint32_t *__restrict__ off) {
+	for (uint32_t c = threadIdx.x + blockIdx.x * blockDim.x; c <= nchunks; c += blockDim.x * gridDim.x) {
+		for (int a = 0; a < 3; a++)
+			off[a * (nchunks + 1) + c] = c < nchunks ? blk[(uint64_t)a * nblocks + chunks[c].blk_off] : totals[a];
+	}
+}
+
+__global__ void __launch_bounds__(DC_T) batch_emit_kernel(const float *__restrict__ d, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ blk_starts, uint32_t nchunks, uint32_t nblocks, const uint32_t *__restrict__ blk, uint32_t *__restrict__ cell_list,
+	uint32_t *__restrict__ cell_map, uint32_t *__restrict__ edge_list, uint32_t *__restrict__ edge_map, uint32_t *__restrict__ quad_list) {
+	const uint32_t c = find_chunk(blk_starts, nchunks, blockIdx.x);
+	const BatchChunkDev &ch = chunks[c];
+	const GridDev g = ch.g;
+	const uint32_t npts = g.n[0] * g.n[1] * g.n[2];
+	const uint32_t base = (blockIdx.x - ch.blk_off) * DC_PB + threadIdx.x * DC_ITEMS;
+	const float *dc = d + ch.pt_off;
+	PointFlags f[DC_ITEMS];
+	uint64_t cnt = 0;
+	#pragma unroll
+	for (int it = 0; it < DC_ITEMS; it++) {
+		const uint32_t p = base + it;
+		f[it].bits = 0;
+		if (p < npts) f[it] = point_flags(dc, g, p);
+		cnt += pack_counts(f[it]);
+	}
+	uint64_t tot;
+	const uint64_t o = block_exscan<DC_T>(cnt, tot);
+	uint32_t co = blk[blockIdx.x] + (uint32_t)(o & 0x1FFFFF);
+	uint32_t eo = blk[nblocks + blockIdx.x] + (uint32_t)((o >> 21) & 0x1FFFFF);
+	uint32_t qo = blk[2 * nblocks + blockIdx.x] + (uint32_t)(o >> 42);
+	const uint32_t nx = g.n[0], ny = g.n[1], cx = nx - 1, cy = ny - 1;
+	uint32_t *cmap = cell_map + ch.cell_off;
+	uint32_t *emap = edge_map + 3 * (uint64_t)ch.pt_off;
+	#pragma unroll
+	for (int it = 0; it < DC_ITEMS; it++) {
+		const uint32_t p = base + it;
+		const uint32_t b = f[it].bits;
+		if (!b) continue;
+		if (b & 1u) {
+			const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
+			cell_list[co] = p;
+			cmap[(k * cy + j) * cx + i] = co;
+			co++;
+		}
+		#pragma unroll
+		for (int a = 0; a < 3; a++)
+			if (b & (2u << a)) {
+				const uint32_t code = 3 * p + a;
+				edge_list[eo] = code;
+				emap[code] = eo;
+				if (b & (16u << a)) quad_list[qo++] = eo;
+				eo++;
+			}
+	}
+}
+
+struct BatchEvalF {
+	const up_synth_program *P;
+	__device__ __forceinline__ NG operator()(V3f p) const { return synth_eval<true, -1, -1>(*P, p); }
+};
+
+__global__ void __launch_bounds__(256) batch_hermite_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ edge_list,
+	double *__restrict__ edge_t, float *__restrict__ edge_n) {
+	const uint32_t *eoff = off + (nchunks + 1);
+	const uint32_t nedges = eoff[nchunks];
+	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nedges; e += gridDim.x * blockDim.x) {
+		const uint32_t c = find_chunk(eoff, nchunks, e);
+		const BatchChunkDev &ch = chunks[c];
+		dc_hermite_item(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, edge_list[e], edge_t[e], edge_n + 3 * (uint64_t)e);
+	}
+}
+
+__global__ void __launch_bounds__(128) batch_qef_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ cell_list,
+	const uint32_t *__restrict__ edge_map, const double *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos) {
+	const uint32_t ncells = off[nchunks];
+	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ncells; q += gridDim.x * blockDim.x) {
+		const uint32_t c = find_chunk(off, nchunks, q);
+		const BatchChunkDev &ch = chunks[c];
+		dc_qef_item(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
+			pos + 3 * (uint64_t)q, nullptr);
+	}
+}
+
+__global__ void __launch_bounds__(256) batch_quads_kernel(const BatchChunkDev *__restrict__ chunks, const uint32_t *__restrict__ off, uint32_t nchunks,
+	const float *__restrict__ d, const uint32_t *__restrict__ quad_list, const uint32_t *__restrict__ edge_list,
+	const uint32_t *__restrict__ cell_map, uint32_t *__restrict__ idx) {
+	const uint32_t *coff = off, *qoff = off + 2 * (nchunks + 1);
+	const uint32_t nquads = qoff[nchunks];
+	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nquads; q += gridDim.x * blockDim.x) {
+		const uint32_t c = find_chunk(qoff, nchunks, q);
+		const BatchChunkDev &ch = chunks[c];
+		dc_quad_item(d + ch.pt_off, ch.g, edge_list[quad_list[q]], cell_map + ch.cell_off, coff[c], idx + 6 * (uint64_t)q);
+	}
+}
+
+// ---------------------------------------------------------------- host side
+void dc_scan_blocks(uint32_t *blk, uint32_t nb, uint32_t *totals, cudaStream_t s);
+
+struct DevBuf {
+	void *p = nullptr;
+	size_t n = 0;
+	cudaError_t ensure(size_t bytes) {
+		if (bytes == 0) bytes = 16;
+		if (n >= bytes) return cudaSuccess;
+		if (p) cudaFree(p);
+		p = nullptr;
+		n = 0;
+		cudaError_t e = cudaMalloc(&p, bytes);
+		if (e == cudaSuccess) n = bytes;
+		return e;
+	}
+	~DevBuf() { if (p) cudaFree(p); }
+	template<class T> T *as() const { return (T *)p; }
+};
+
+struct BatchState {
+	std::vector<uint8_t> key;      // bytes of (planets, chunks) of the planned input
+	uint32_t nchunks = 0, npts = 0, ncells_all = 0, nblocks = 0, ntiles = 0;
+	uint32_t ncells = 0, nedges = 0, nquads = 0;
+	int threads = 256;             // autotuned sampling block size
+	DevBuf planets, chunks, tiles, blkst, grid, blk, totals, off, cmap, emap, clist, elist, qlist, et, en, pos, idx, counter, flag;
+	cudaStream_t stream = nullptr;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	~BatchState() {
+		if (exec) cudaGraphExecDestroy(exec);
+		if (graph) cudaGraphDestroy(graph);
+		if (stream) cudaStreamDestroy(stream);
+	}
+};
+
+static int sample_blocks(int threads) {
+	const void *k = threads == 128 ? (const void *)batch_sample_kernel<128> : (threads == 512 ? (const void *)batch_sample_kernel<512> : (const void *)batch_sample_kernel<256>);
+	return persistent_blocks(k, threads);
+}
+
+static cudaError_t enqueue_sample(BatchState &S, int threads, cudaStream_t s) {
+	cudaError_t e = cudaMemsetAsync(S.counter.p, 0, 4, s);
+	if (e != cudaSuccess) return e;
+	const int b = sample_blocks(threads);
+	const auto *P = S.planets.as<up_synth_program>();
+	const auto *C = S.chunks.as<BatchChunkDev>();
+	if (threads == 128) batch_sample_kernel<128><<<b, 128, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	else if (threads == 512) batch_sample_kernel<512><<<b, 512, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	else batch_sample_kernel<256><<<b, 256, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	return cudaGetLastError();
+}
+
+static cudaError_t enqueue_front(BatchState &S, cudaStream_t s) {
+	cudaError_t e = enqueue_sample(S, S.threads, s);
+	if (e != cudaSuccess) return e;
+	batch_count_kernel<<<S.nblocks, DC_T, 0, s>>>(S.grid.as<float>(), S.chunks.as<BatchChunkDev>(), S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>());
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	dc_scan_blocks(S.blk.as<uint32_t>(), S.nblocks, S.totals.as<uint32_t>(), s);
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	batch_offsets_kernel<<<(S.nchunks + 256) / 256, 256, 0, s>>>(S.chunks.as<BatchChunkDev>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>(), S.totals.as<uint32_t>(), S.off.as<uint32_t>());
+	return cudaGetLastError();
+}
+
+static cudaError_t enqueue_back(BatchState &S, cudaStream_t s) {
+	const auto *P = S.planets.as<up_synth_program>();
+	const auto *C = S.chunks.as<BatchChunkDev>();
+	batch_emit_kernel<<<S.nblocks, DC_T, 0, s>>>(S.grid.as<float>(), C, S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>(),
+		S.clist.as<uint32_t>(), S.cmap.as<uint32_t>(), S.elist.as<uint32_t>(), S.emap.as<uint32_t>(), S.qlist.as<uint32_t>());
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	auto grid_of = [](const void *k, int t, uint32_t work) {
+		const int b = persistent_blocks(k, t);
+		const uint32_t need = (work + t - 1) / t;
+		return need < (uint32_t)b ? (need ? need : 1u) : (uint32_t)b;
+	};
+	batch_hermite_kernel<<<grid_of((const void *)batch_hermite_kernel, 256, S.nedges), 256, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks,
+		S.grid.as<float>(), S.elist.as<uint32_t>(), S.et.as<double>(), S.en.as<float>());
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	batch_qef_kernel<<<grid_of((const void *)batch_qef_kernel, 128, S.ncells), 128, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
+		S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<double>(), S.en.as<float>(), S.pos.as<float>());
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	batch_quads_kernel<<<grid_of((const void *)batch_quads_kernel, 256, S.nquads), 256, 0, s>>>(C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
+		S.qlist.as<uint32_t>(), S.elist.as<uint32_t>(), S.cmap.as<uint32_t>(), S.idx.as<uint32_t>());
+	return cudaGetLastError();
+}
+
+void batch_state_free(void *p) { delete (BatchState *)p; }
+
+// Plans (or reuses) the batch for this input and runs it; on return the
+// device outputs are in the state's pos/idx buffers and counts are filled.
+// Returns cudaSuccess or an error; *nan set when a sample was NaN.
+cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks,
+	uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
+	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, cudaStream_t caller) {
+	std::vector<uint8_t> key(nplanets * sizeof(up_synth_program) + nchunks * sizeof(up_chunk));
+	std::memcpy(key.data(), planets, nplanets * sizeof(up_synth_program));
+	std::memcpy(key.data() + nplanets * sizeof(up_synth_program), chunks, nchunks * sizeof(up_chunk));
+	BatchState *S = (BatchState *)state;
+	cudaError_t e;
+	replayed = false;
+	if (S && S->key == key && S->exec) {
+		// replay: the same work, recomputed, ordered after the caller's stream
+		cudaEvent_t ev;
+		if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+		cudaEventRecord(ev, caller);
+		cudaStreamWaitEvent(S->stream, ev, 0);
+		e = cudaGraphLaunch(S->exec, S->stream);
+		cudaEventRecord(ev, S->stream);
+		cudaStreamWaitEvent(caller, ev, 0);
+		cudaEventDestroy(ev);
+		if (e != cudaSuccess) return e;
+		replayed = true;
+	} else {
+		if (S) { delete S; state = nullptr; }
+		S = new BatchState();
+		state = S;
+		S->key = key;
+		if ((e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)) != cudaSuccess) return e;
+		// host chunk table
+		std::vector<BatchChunkDev> tab(nchunks);
+		std::vector<uint32_t> tiles(nchunks), blks(nchunks);
+		uint64_t pts = 0, cells = 0, nb = 0, nt = 0;
+		for (size_t c = 0; c < nchunks; c++) {
+			BatchChunkDev &t = tab[c];
+			t.g = make_grid(chunks[c].grid);
+			t.planet = chunks[c].planet;
+			const uint64_t n = (uint64_t)t.g.n[0] * t.g.n[1] * t.g.n[2];
+			t.pt_off = (uint32_t)pts;
+			t.cell_off = (uint32_t)cells;
+			t.blk_off = (uint32_t)nb;
+			t.tile_off = (uint32_t)nt;
+			tiles[c] = t.tile_off;
+			blks[c] = t.blk_off;
+			pts += n;
+			cells += (uint64_t)(t.g.n[0] - 1) * (t.g.n[1] - 1) * (t.g.n[2] - 1);
+			nb += (n + DC_PB - 1) / DC_PB;
+			nt += (n + BATCH_TILE - 1) / BATCH_TILE;
+		}
+		if (3 * pts >= (1ull << 32)) return cudaErrorInvalidValue;
+		S->nchunks = (uint32_t)nchunks; S->npts = (uint32_t)pts; S->ncells_all = (uint32_t)cells; S->nblocks = (uint32_t)nb; S->ntiles = (uint32_t)nt;
+		if ((e = S->planets.ensure(nplanets * sizeof(up_synth_program))) != cudaSuccess) return e;
+		if ((e = S->chunks.ensure(nchunks * sizeof(BatchChunkDev))) != cudaSuccess) return e;
+		if ((e = S->tiles.ensure(nchunks * 4)) != cudaSuccess) return e;
+		if ((e = S->blkst.ensure(nchunks * 4)) != cudaSuccess) return e;
+		if ((e = S->grid.ensure(pts * 4)) != cudaSuccess) return e;
+		if ((e = S->blk.ensure(nb * 12)) != cudaSuccess) return e;
+		if ((e = S->totals.ensure(16)) != cudaSuccess) return e;
+		if ((e = S->off.ensure((nchunks + 1) * 12)) != cudaSuccess) return e;
+		if ((e = S->cmap.ensure(cells * 4)) != cudaSuccess) return e;
+		if ((e = S->emap.ensure(pts * 12)) != cudaSuccess) return e;
+		if ((e = S->counter.ensure(16)) != cudaSuccess) return e;
+		if ((e = S->flag.ensure(16)) != cudaSuccess) return e;
+		cudaStream_t s = S->stream;
+		cudaEvent_t ev;
+		if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+		cudaEventRecord(ev, caller);
+		cudaStreamWaitEvent(s, ev, 0);
+		cudaEventDestroy(ev);
+		cudaMemcpyAsync(S->planets.p, planets, nplanets * sizeof(up_synth_program), cudaMemcpyHostToDevice, s);
+		cudaMemcpyAsync(S->chunks.p, tab.data(), nchunks * sizeof(BatchChunkDev), cudaMemcpyHostToDevice, s);
+		cudaMemcpyAsync(S->tiles.p, tiles.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
+		cudaMemcpyAsync(S->blkst.p, blks.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
+		cudaMemsetAsync(S->flag.p, 0, 4, s);
+		// autotune the sampling block size (each candidate runs the full sampling stage once)
+		{
+			cudaEvent_t a, b;
+			cudaEventCreate(&a);
+			cudaEventCreate(&b);
+			float best = 1e30f;
+			for (int t : {128, 256, 512}) {
+				cudaEventRecord(a, s);
+				if ((e = enqueue_sample(*S, t, s)) != cudaSuccess) break;
+				cudaEventRecord(b, s);
+				cudaEventSynchronize(b);
+				float ms = 0.f;
+				cudaEventElapsedTime(&ms, a, b);
+				if (ms < best) { best = ms; S->threads = t; }
+			}
+			cudaEventDestroy(a);
+			cudaEventDestroy(b);
+			if (e != cudaSuccess) return e;
+		}
+		if ((e = enqueue_front(*S, s)) != cudaSuccess) return e;
+		uint32_t tot[4] = {0, 0, 0, 0};
+		cudaMemcpyAsync(tot, S->totals.p, 12, cudaMemcpyDeviceToHost, s);
+		if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+		S->ncells = tot[0]; S->nedges = tot[1]; S->nquads = tot[2];
+		if ((e = S->clist.ensure((size_t)S->ncells * 4)) != cudaSuccess) return e;
+		if ((e = S->elist.ensure((size_t)S->nedges * 4)) != cudaSuccess) return e;
+		if ((e = S->qlist.ensure((size_t)S->nquads * 4)) != cudaSuccess) return e;
+		if ((e = S->et.ensure((size_t)S->nedges * 8)) != cudaSuccess) return e;
+		if ((e = S->en.ensure((size_t)S->nedges * 12)) != cudaSuccess) return e;
+		if ((e = S->pos.ensure((size_t)S->ncells * 12)) != cudaSuccess) return e;
+		if ((e = S->idx.ensure((size_t)S->nquads * 24)) != cudaSuccess) return e;
+		if ((e = enqueue_back(*S, s)) != cudaSuccess) return e;
+		if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+		// capture every stage for replays of the same input
+		if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+		cudaError_t e1 = cudaMemsetAsync(S->flag.p, 0, 4, s);
+		if (e1 == cudaSuccess) e1 = enqueue_front(*S, s);
+		if (e1 == cudaSuccess) e1 = enqueue_back(*S, s);
+		e = cudaStreamEndCapture(s, &S->graph);
+		if (e1 != cudaSuccess) return e1;
+		if (e != cudaSuccess) return e;
+		if ((e = cudaGraphInstantiate(&S->exec, S->graph, 0)) != cudaSuccess) return e;
+		cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+		cudaEventRecord(ev, s);
+		cudaStreamWaitEvent(caller, ev, 0);
+		cudaEventDestroy(ev);
+	}
+	// per-chunk offsets and the NaN flag
+	std::vector<uint32_t> off(3 * (S->nchunks + 1));
+	unsigned fl = 0;
+	cudaMemcpyAsync(off.data(), S->off.p, off.size() * 4, cudaMemcpyDeviceToHost, S->stream);
+	cudaMemcpyAsync(&fl, S->flag.p, 4, cudaMemcpyDeviceToHost, S->stream);
+	if ((e = cudaStreamSynchronize(S->stream)) != cudaSuccess) return e;
+	chunk_cells.assign(off.begin(), off.begin() + S->nchunks + 1);
+	chunk_quads.assign(off.begin() + 2 * (S->nchunks + 1), off.end());
+	ncells = S->ncells;
+	nquads = S->nquads;
+	dpos = S->pos.as<float>();
+	didx = S->idx.as<uint32_t>();
+	dvalues = S->grid.as<float>();
+	nvalues = S->npts;
+	nan = fl != 0;
+	return cudaSuccess;
+}
+
+} // namespace up

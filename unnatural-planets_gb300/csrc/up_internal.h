@@ -20,8 +20,8 @@ struct ModesDesc;
 // ---- SDF sampling (up_sdf.cu / up_modes.cu)
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
-cudaError_t launch_modes_grid(const ModesDesc &M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag, cudaStream_t s);
-cudaError_t launch_modes_points(const ModesDesc &M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
+cudaError_t launch_modes_grid(const ModesDesc *M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag, cudaStream_t s);
+cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 
 // adjoint: partial sums per block into partials (nblocks x ACC stride), then
 // a fixed-order reduction into dtheta (compact layout)
@@ -48,7 +48,7 @@ cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_
 cudaError_t dc_emit(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s);
 cudaError_t dc_geometry_synth(const up_synth_program &P, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells, uint32_t nedges,
 	uint32_t nquads, float *pos, float *nrm, uint32_t *idx, cudaStream_t s);
-cudaError_t dc_geometry_modes(const ModesDesc &M, int field, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells,
+cudaError_t dc_geometry_modes(const ModesDesc *M, int field, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells,
 	uint32_t nedges, uint32_t nquads, float *pos, float *nrm, uint32_t *idx, cudaStream_t s);
 
 // occupancy-derived persistent grid size

@@ -24,8 +24,10 @@
 
 #ifdef __CUDACC__
 #define UP_HD __host__ __device__ __forceinline__
+#define UP_HD_OUTLINE static __host__ __device__ __noinline__
 #else
 #define UP_HD inline
+#define UP_HD_OUTLINE static inline
 #endif
 
 namespace up {
@@ -283,10 +285,10 @@ UP_HD NG cellular_n(V3f p, uint32_t key, int dist_rt, int op_rt) {
 	float F1 = 1e20f, F2 = 1e20f;
 	V3f g1 = zero3(), g2 = zero3();
 	uint32_t cellh = 0;
-	#pragma unroll
+	#pragma unroll 1
 	for (int dz = -1; dz <= 1; dz++) {
 		const uint32_t zh = ((uint32_t)(c.iz + dz) * HZ) ^ key;
-		#pragma unroll
+		#pragma unroll 1
 		for (int dy = -1; dy <= 1; dy++) {
 			const uint32_t yzh = ((uint32_t)(c.iy + dy) * HY) ^ zh;
 			#pragma unroll
@@ -330,9 +332,10 @@ UP_HD NG cellular_n(V3f p, uint32_t key, int dist_rt, int op_rt) {
 }
 
 // ---------------------------------------------------------------- dispatch
-// noise type codes follow up_noise_type in include/up_abi.h
+// noise type codes follow up_noise_type in include/up_abi.h; the run-time
+// dispatch is out of line (one copy per translation unit and GRAD)
 template<bool GRAD>
-UP_HD NG noise_single(int type, V3f p, uint32_t key, int dist, int op) {
+UP_HD_OUTLINE NG noise_single(int type, V3f p, uint32_t key, int dist, int op) {
 	switch (type) {
 		case 0: if (GRAD) return value_g(p, key); return ngc(value_v(p, key));
 		case 1: return cubic_n<GRAD>(p, key);

@@ -1,0 +1,233 @@
+// Texel pipeline of an unwrapped mesh: UV rasterisation, per-texel coloring,
+// dilation and 8-bit quantisation; plus batched tiles for points.
+//
+// Replaces Generator<Water>::generate (sources/textures.cpp:45-82): the cage
+// rasteriser meshGenerateTexture (:66-71) calling Generator::pixel (:24-43)
+// for every covered texel, imageDilation(7) (:73-77) and imageConvert U8
+// (:79-81); and the per-vertex terrainTile loop of
+// sources/tileProperties.cpp:256-273.
+//
+// Rasterisation rule (the oracle implements the same): vertices snapped to
+// 1/256 texel in int64 fixed point, texel centres at (x+0.5, y+0.5), exact
+// edge functions; a texel on an edge belongs to the triangle (oriented to
+// positive area) for which the edge has dy > 0, or dy == 0 and dx < 0;
+// overlaps go to the highest triangle id (atomicMax). Barycentric weights
+// and the interpolation of position and normal are FP64.
+#include "up_internal.h"
+#include "up_coloring.cuh"
+
+namespace up {
+
+struct TexMesh {
+	const float *pos, *nrm, *uv;
+	const uint32_t *idx;
+	uint64_t ntri;
+};
+
+struct FixTri {
+	long long ax, ay, bx, by, cx, cy, area;
+	int o[3];
+};
+__device__ __forceinline__ bool tri_fixed(const TexMesh &m, uint64_t t, uint32_t W, uint32_t H, FixTri &f) {
+	long long X[3], Y[3];
+	#pragma unroll
+	for (int k = 0; k < 3; k++) {
+		const uint32_t v = m.idx[3 * t + k];
+		X[k] = __double2ll_rn((double)m.uv[2 * (uint64_t)v] * (double)W * 256.0);
+		Y[k] = __double2ll_rn((double)m.uv[2 * (uint64_t)v + 1] * (double)H * 256.0);
+	}
+	long long area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+	if (area == 0) return false;
+	f.o[0] = 0; f.o[1] = 1; f.o[2] = 2;
+	if (area < 0) { f.o[1] = 2; f.o[2] = 1; area = -area; }
+	f.ax = X[f.o[0]]; f.ay = Y[f.o[0]]; f.bx = X[f.o[1]]; f.by = Y[f.o[1]]; f.cx = X[f.o[2]]; f.cy = Y[f.o[2]];
+	f.area = area;
+	return true;
+}
+__device__ __forceinline__ bool edge_in(long long e, long long dx, long long dy) { return e > 0 || (e == 0 && (dy > 0 || (dy == 0 && dx < 0))); }
+__device__ __forceinline__ bool tri_cover(const FixTri &f, long long px, long long py, long long e[3]) {
+	e[0] = (f.cx - f.bx) * (py - f.by) - (f.cy - f.by) * (px - f.bx);
+	e[1] = (f.ax - f.cx) * (py - f.cy) - (f.ay - f.cy) * (px - f.cx);
+	e[2] = (f.bx - f.ax) * (py - f.ay) - (f.by - f.ay) * (px - f.ax);
+	return edge_in(e[0], f.cx - f.bx, f.cy - f.by) && edge_in(e[1], f.ax - f.cx, f.ay - f.cy) && edge_in(e[2], f.bx - f.ax, f.by - f.ay);
+}
+
+__global__ void __launch_bounds__(256) tex_raster_kernel(const TexMesh m, uint32_t W, uint32_t H, int *__restrict__ owner) {
+	for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m.ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+		FixTri f;
+		if (!tri_fixed(m, t, W, H, f)) continue;
+		const long long xmin = min(f.ax, min(f.bx, f.cx)), xmax = max(f.ax, max(f.bx, f.cx));
+		const long long ymin = min(f.ay, min(f.by, f.cy)), ymax = max(f.ay, max(f.by, f.cy));
+		// texel x is covered only if x*256 + 128 lies in [xmin, xmax]
+		const long long tx0 = max(0ll, (xmin - 128 + 255) >> 8), tx1 = min((long long)W - 1, (xmax - 128) >> 8);
+		const long long ty0 = max(0ll, (ymin - 128 + 255) >> 8), ty1 = min((long long)H - 1, (ymax - 128) >> 8);
+		for (long long y = ty0; y <= ty1; y++)
+			for (long long x = tx0; x <= tx1; x++) {
+				long long e[3];
+				if (tri_cover(f, x * 256 + 128, y * 256 + 128, e)) atomicMax(owner + (uint64_t)y * W + x, (int)t);
+			}
+	}
+}
+
+// per texel: interpolate position and normal of the owning triangle, color
+template<bool SYNTH>
+__global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_t W, uint32_t H, const int *__restrict__ owner,
+	const ModesDesc *__restrict__ Mp, const up_synth_program P, int purpose, float *__restrict__ img, int ach) {
+	const int nch = ach + 3;
+	const uint64_t n = (uint64_t)W * H;
+	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (uint64_t)gridDim.x * blockDim.x) {
+		float *o = img + q * nch;
+		const int t = owner[q];
+		if (t < 0) {
+			for (int c = 0; c < nch; c++) o[c] = NAN;
+			continue;
+		}
+		FixTri f;
+		tri_fixed(m, (uint64_t)t, W, H, f);
+		long long e[3];
+		const uint32_t x = (uint32_t)(q % W), y = (uint32_t)(q / W);
+		tri_cover(f, (long long)x * 256 + 128, (long long)y * 256 + 128, e);
+		double w[3];
+		w[f.o[0]] = (double)e[0] / (double)f.area;
+		w[f.o[1]] = (double)e[1] / (double)f.area;
+		w[f.o[2]] = (double)e[2] / (double)f.area;
+		double p[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
+		#pragma unroll
+		for (int k = 0; k < 3; k++) {
+			const uint64_t v = m.idx[3 * (uint64_t)t + k];
+			#pragma unroll
+			for (int a = 0; a < 3; a++) {
+				p[a] += (double)m.pos[3 * v + a] * w[k];
+				nn[a] += (double)m.nrm[3 * v + a] * w[k];
+			}
+		}
+		const double ln = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+		const V3f pf = v3((float)p[0], (float)p[1], (float)p[2]);
+		const V3f nf = v3((float)(nn[0] / ln), (float)(nn[1] / ln), (float)(nn[2] / ln));
+		V3f albedo;
+		float rough, metal = 0.f, height, opacity = 1.f;
+		if (SYNTH) {
+			synth_texel(P, pf, albedo, rough, height);
+		} else {
+			TileD tl = tile_init(pf, nf, purpose);
+			color_tile(*Mp, tl);
+			albedo = tl.albedo; rough = tl.roughness; metal = tl.metallic; height = tl.height; opacity = tl.opacity;
+		}
+		o[0] = albedo.x; o[1] = albedo.y; o[2] = albedo.z;
+		if (ach == 4) o[3] = opacity;
+		o[ach] = rough; o[ach + 1] = metal; o[ach + 2] = height;
+	}
+}
+
+// one dilation round over all channels (shared coverage): a NaN texel with
+// valid 8-neighbours becomes their mean
+__global__ void __launch_bounds__(256) tex_dilate_kernel(const float *__restrict__ src, float *__restrict__ dst, uint32_t W, uint32_t H, int nch) {
+	const uint64_t n = (uint64_t)W * H;
+	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (uint64_t)gridDim.x * blockDim.x) {
+		const float *s = src + q * nch;
+		float *d = dst + q * nch;
+		if (!isnan(s[0])) {
+			for (int c = 0; c < nch; c++) d[c] = s[c];
+			continue;
+		}
+		const int x = (int)(q % W), y = (int)(q / W);
+		float acc[7] = {0, 0, 0, 0, 0, 0, 0};
+		int cnt = 0;
+		for (int dy = -1; dy <= 1; dy++)
+			for (int dx = -1; dx <= 1; dx++) {
+				if (!dx && !dy) continue;
+				const int xx = x + dx, yy = y + dy;
+				if (xx < 0 || yy < 0 || xx >= (int)W || yy >= (int)H) continue;
+				const float *r = src + ((uint64_t)yy * W + xx) * nch;
+				if (isnan(r[0])) continue;
+				for (int c = 0; c < nch; c++) acc[c] += r[c];
+				cnt++;
+			}
+		const float ic = cnt ? 1.f / (float)cnt : 0.f;
+		for (int c = 0; c < nch; c++) d[c] = cnt ? acc[c] * ic : NAN;
+	}
+}
+
+__device__ __forceinline__ uint8_t to_u8(float v) { return isnan(v) ? (uint8_t)0 : (uint8_t)(fminf(fmaxf(v, 0.f), 1.f) * 255.f + 0.5f); }
+
+// split the interleaved working image into the caller's images
+__global__ void __launch_bounds__(256) tex_output_kernel(const float *__restrict__ img, uint64_t n, int ach, uint8_t *__restrict__ a8,
+	uint8_t *__restrict__ s8, uint8_t *__restrict__ h8, float *__restrict__ af, float *__restrict__ sf, float *__restrict__ hf) {
+	const int nch = ach + 3;
+	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (uint64_t)gridDim.x * blockDim.x) {
+		const float *s = img + q * nch;
+		for (int c = 0; c < ach; c++) {
+			if (a8) a8[q * ach + c] = to_u8(s[c]);
+			if (af) af[q * ach + c] = s[c];
+		}
+		if (s8) { s8[2 * q] = to_u8(s[ach]); s8[2 * q + 1] = to_u8(s[ach + 1]); }
+		if (sf) { sf[2 * q] = s[ach]; sf[2 * q + 1] = s[ach + 1]; }
+		if (h8) h8[q] = to_u8(s[ach + 2]);
+		if (hf) hf[q] = s[ach + 2];
+	}
+}
+
+// tiles as SoA planes: out[k * n + i] for the 11 float channels (albedo r,
+// g, b, roughness, metallic, height, opacity, elevation, slope, temperature,
+// precipitation), bt[i] = biome, bt[n + i] = type
+__global__ void __launch_bounds__(128) tiles_kernel(const ModesDesc *__restrict__ Mp, int purpose, const float *__restrict__ pos,
+	const float *__restrict__ nrm, uint64_t n, float *__restrict__ out, uint8_t *__restrict__ bt) {
+	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+		TileD t = tile_init(v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), v3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]), purpose);
+		color_tile(*Mp, t);
+		const float v[11] = {t.albedo.x, t.albedo.y, t.albedo.z, t.roughness, t.metallic, t.height, t.opacity, t.elevation, t.slope,
+			t.temperature, t.precipitation};
+		#pragma unroll
+		for (int k = 0; k < 11; k++) out[k * n + i] = v[k];
+		bt[i] = (uint8_t)t.biome;
+		bt[n + i] = (uint8_t)t.type;
+	}
+}
+
+static int blocks_for(const void *k, int threads, uint64_t work) {
+	int b = persistent_blocks(k, threads);
+	const uint64_t need = (work + threads - 1) / threads;
+	if ((uint64_t)b > need) b = (int)(need ? need : 1);
+	return b;
+}
+
+cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int purpose, const float *pos, const float *nrm, const float *uv,
+	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, int *owner, float *img0, float *img1, uint8_t *a8, uint8_t *s8,
+	uint8_t *h8, float *af, float *sf, float *hf, int *launches, cudaStream_t s) {
+	const uint64_t n = (uint64_t)W * H;
+	const int ach = purpose == UP_PURPOSE_WATER ? 4 : 3;
+	const int nch = ach + 3;
+	TexMesh m{pos, nrm, uv, idx, nidx / 3};
+	cudaError_t e = cudaMemsetAsync(owner, 0xFF, n * sizeof(int), s);
+	if (e != cudaSuccess) return e;
+	int L = 0;
+	if (m.ntri) {
+		tex_raster_kernel<<<blocks_for((const void *)tex_raster_kernel, 256, m.ntri), 256, 0, s>>>(m, W, H, owner);
+		L++;
+	}
+	up_synth_program P{};
+	if (synth) {
+		P = *synth;
+		tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+	} else {
+		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+	}
+	L++;
+	float *cur = img0, *nxt = img1;
+	for (int r = 0; r < dilation; r++) {
+		tex_dilate_kernel<<<blocks_for((const void *)tex_dilate_kernel, 256, n), 256, 0, s>>>(cur, nxt, W, H, nch);
+		L++;
+		float *t = cur; cur = nxt; nxt = t;
+	}
+	tex_output_kernel<<<blocks_for((const void *)tex_output_kernel, 256, n), 256, 0, s>>>(cur, n, ach, a8, s8, h8, af, sf, hf);
+	L++;
+	if (launches) *launches = L;
+	return cudaGetLastError();
+}
+
+cudaError_t tiles_run(const ModesDesc *M, int purpose, const float *pos, const float *nrm, uint64_t n, float *out11, uint8_t *bt, cudaStream_t s) {
+	tiles_kernel<<<blocks_for((const void *)tiles_kernel, 128, n), 128, 0, s>>>(M, purpose, pos, nrm, n, out11, bt);
+	return cudaGetLastError();
+}
+
+} // namespace up

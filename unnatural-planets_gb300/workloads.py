@@ -130,3 +130,59 @@ def shell_points(P_radius: float, thickness: float, n: int, seed: int) -> np.nda
 # FMA counts 2; besides these, 8 divisions, 37 square roots and 21 floors per
 # sample are counted apart and not included). Checked by tests/test_oracle.py.
 FLOPS_PER_SAMPLE_C2 = 960.8
+
+
+def quad_atlas(pos: np.ndarray, nrm: np.ndarray, idx: np.ndarray, width: int, height: int):
+    """Test/benchmark stand-in for the reference's meshUnwrap (which stays on
+    the CPU): every dual-contouring quad (two consecutive triangles sharing a
+    diagonal) gets its own square chart in a regular grid of the atlas, with
+    half a texel of margin. Returns (positions, normals, uvs, indices) with
+    four vertices per quad."""
+    tri = idx.reshape(-1, 6).astype(np.int64)
+    q = len(tri)
+    a, b = tri[:, :3], tri[:, 3:]
+    # diagonal = the two vertices the triangles share; v1/v3 = the others
+    in_b = (a[:, :, None] == b[:, None, :]).any(axis=2)          # (q, 3) which of a's vertices are in b
+    in_a = (b[:, :, None] == a[:, None, :]).any(axis=2)
+    v1 = a[np.arange(q), np.argmin(in_b, axis=1)]
+    v3 = b[np.arange(q), np.argmin(in_a, axis=1)]
+    diag = np.where(in_b, a, -1)
+    v0 = diag.max(axis=1)
+    v2 = np.where(diag == v0[:, None], -1, diag).max(axis=1)
+    corners = np.stack([v0, v1, v2, v3], axis=1)                  # (q, 4)
+    cells = int(np.ceil(np.sqrt(q))) if q else 1
+    s = min(width, height) // cells
+    if s < 2:
+        raise ValueError("atlas too small for one chart of at least 2x2 texels per quad")
+    tx, ty = np.arange(q) % cells, np.arange(q) // cells
+    cu = np.array([0.0, 1.0, 1.0, 0.0])
+    cv = np.array([0.0, 0.0, 1.0, 1.0])
+    u = (tx[:, None] * s + 0.5 + cu[None, :] * (s - 1.0)) / width
+    v = (ty[:, None] * s + 0.5 + cv[None, :] * (s - 1.0)) / height
+    P = pos[corners.reshape(-1)].astype(np.float32)
+    N = nrm[corners.reshape(-1)].astype(np.float32)
+    UV = np.stack([u.reshape(-1), v.reshape(-1)], axis=1).astype(np.float32)
+    base = 4 * np.arange(q, dtype=np.uint32)[:, None]
+    I = (base + np.array([0, 1, 2, 0, 2, 3], np.uint32)[None, :]).reshape(-1).astype(np.uint32)
+    return P, N, UV, I
+
+
+def chunk_set(n_planets=64, n_chunks=512, seed=7, edge_lo=16, edge_hi=192):
+    """Batched-chunk workload: n_planets mixed planets (mixed_planet) and
+    n_chunks chunks whose per-axis sample counts are log-uniform in
+    [edge_lo, edge_hi]; every chunk box has the grid spacing 2.6/191 and is
+    centred near a random point of the unit sphere (so most chunks cut the
+    surface). Returns (planets list, list of (planet index, Grid))."""
+    rng = np.random.default_rng(seed)
+    planets = [mixed_planet(rng) for _ in range(n_planets)]
+    h = 2.6 / 191.0
+    chunks = []
+    for _ in range(n_chunks):
+        p = int(rng.integers(0, n_planets))
+        n = np.exp(rng.uniform(np.log(edge_lo), np.log(edge_hi), size=3)).astype(int)
+        d = rng.normal(size=3)
+        centre = d / np.linalg.norm(d) * rng.uniform(0.8, 1.1)
+        lo = centre - 0.5 * (n - 1) * h
+        hi = lo + (n - 1) * h
+        chunks.append((p, abi.Grid.make(lo.tolist(), hi.tolist(), n.tolist())))
+    return planets, chunks
