@@ -3,6 +3,7 @@
 // GPU. It exercises arithmetic only; the kernels themselves run in the GPU
 // tests. Built by tests/hostcheck/build_hostcheck.py into tests/hostcheck/_build.
 #include "../../unnatural-planets_gb300/csrc/up_synth.cuh"
+#include "../../unnatural-planets_gb300/csrc/up_grid_runs.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_modes.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_coloring.cuh"
 #include <string>
@@ -104,5 +105,38 @@ void hc_synth_texel(const up_synth_program *P, const float *pos, uint64_t n, flo
 		synth_texel(*P, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), a, r, h);
 		out5[5 * i] = a.x; out5[5 * i + 1] = a.y; out5[5 * i + 2] = a.z; out5[5 * i + 3] = r; out5[5 * i + 4] = h;
 	}
+}
+
+// whole grid of the torus/spheres/ridged-Perlin/cellular program through the
+// run-based evaluation (runs of RUN_R samples along x, the kernel's order)
+void hc_grid_runs(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float *out, float *grad) {
+	constexpr int R = RUN_R;
+	constexpr int T1 = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);
+	const uint64_t plane = (uint64_t)n[0] * n[1] * n[2];
+	auto coord = [&](int a, uint32_t i) { volatile float m = (float)i * step[a]; return m + lo[a]; };
+	RunCtx rc;
+	rc.lo_x = lo[0];
+	rc.step_x = step[0];
+	rc.nx = n[0];
+	for (uint32_t k = 0; k < n[2]; k++)
+		for (uint32_t j = 0; j < n[1]; j++)
+			for (uint32_t i0 = 0; i0 < n[0]; i0 += R) {
+				rc.i0 = i0;
+				rc.py = coord(1, j);
+				rc.pz = coord(2, k);
+				if (grad) {
+					Acc4 acc[R];
+					synth_run<true, 2, T1>(*P, rc, R, acc, 1);
+					for (int r = 0; r < R && i0 + r < n[0]; r++) {
+						const uint64_t idx = ((uint64_t)k * n[1] + j) * n[0] + i0 + r;
+						out[idx] = acc[r].v;
+						grad[idx] = acc[r].gx; grad[plane + idx] = acc[r].gy; grad[2 * plane + idx] = acc[r].gz;
+					}
+				} else {
+					float acc[R];
+					synth_run<false, 2, T1>(*P, rc, R, acc, 1);
+					for (int r = 0; r < R && i0 + r < n[0]; r++) out[((uint64_t)k * n[1] + j) * n[0] + i0 + r] = acc[r];
+				}
+			}
 }
 }

@@ -1,0 +1,281 @@
+// x-coherent grid sampling of synthetic programs ("runs").
+//
+// A warp evaluates RUN_R consecutive samples along x for 32 different (y, z)
+// rows: every lane sees the same x coordinates, so a lattice-cell change
+// along x happens for all lanes at the same sample (warp-uniform control
+// flow). Per-sample accumulators (value and gradient) live in shared memory
+// as acc[r * stride + lane-slot], so the sample loops stay rolled and
+// every code block appears once (the unrolled form overflowed the
+// instruction cache).
+// Lattice noise (value, Perlin): per octave, the y/z fade weights are formed
+// once per run; the 8 corner hashes and gradients are formed only when the
+// x cell changes (once per segment of samples sharing a cell) and folded
+// into 12 coefficients (x halves h = 0/1 of
+//   A_h(t) = t GX_h + C_h,  dA_h/dy = t P_hy + Q_hy,  dA_h/dz = t P_hz + Q_hz),
+// after which a sample's value and analytic gradient cost a few FMAs:
+//   n = A0(fx) + u (A1(fx - 1) - A0(fx)),
+//   dn/dx = GX0 + u (GX1 - GX0) + u' (A1 - A0), dn/dy, dn/dz likewise
+// (the trilinear form of I. Quilez's gradient-noise derivatives).
+// Cellular noise: in sub-runs of 8 samples, candidates outer and samples
+// inner -- each of the 3 or 4 x columns of 9 candidate cells is hashed once
+// per sub-run, a sample ignores columns outside its own 3x3x3 neighbourhood
+// (so results equal the per-sample search); F1/F2 are tracked by squared
+// length and candidate id, and the winners' difference vectors are rebuilt
+// for the gradient.
+// Results equal the per-sample kernels up to FP32 reassociation.
+#pragma once
+#include "up_synth.cuh"
+
+namespace up {
+
+constexpr int RUN_R = 16;   // samples per run
+constexpr int CELL_SUB = 8; // cellular sub-run
+
+// sample coordinates of a run: x(r) = lo + (i0 + r) step (clamped to the grid)
+struct RunCtx {
+	float lo_x, step_x;
+	uint32_t i0, nx;
+	float py, pz;
+	UP_HD float px(int r) const {
+		const uint32_t i = i0 + (uint32_t)r < nx ? i0 + (uint32_t)r : nx - 1;
+#ifdef __CUDA_ARCH__
+		return __fadd_rn(__fmul_rn((float)i, step_x), lo_x);
+#else
+		volatile float m = (float)i * step_x;
+		return m + lo_x;
+#endif
+	}
+};
+
+// per-sample accumulator: value and gradient (Acc4) or value only (float);
+// acc[r * stride] belongs to sample r
+struct alignas(16) Acc4 { float v, gx, gy, gz; };
+template<bool GRAD> struct AccOf { typedef Acc4 T; };
+template<> struct AccOf<false> { typedef float T; };
+UP_HD void acc_set(Acc4 *a, int i, float v, float gx, float gy, float gz) { Acc4 t; t.v = v; t.gx = gx; t.gy = gy; t.gz = gz; a[i] = t; }
+UP_HD void acc_set(float *a, int i, float v, float, float, float) { a[i] = v; }
+UP_HD void acc_add(Acc4 *a, int i, float v, float gx, float gy, float gz) {
+	Acc4 t = a[i];
+	t.v += v; t.gx += gx; t.gy += gy; t.gz += gz;
+	a[i] = t;
+}
+UP_HD void acc_add(float *a, int i, float v, float, float, float) { a[i] += v; }
+
+// one octave of lattice noise (VALUE = value noise, else Perlin); subtracts
+// amp * s(n) (s = n or 1 - 2|n|) from every sample of the run
+template<bool GRAD, bool VALUE>
+UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
+	const float qy = rc.py * f, qz = rc.pz * f;
+	const float fy0 = floorf(qy), fz0 = floorf(qz);
+	const int iy = (int)fy0, iz = (int)fz0;
+	const float fy = qy - fy0, fz = qz - fz0;
+	const float v = fade(fy), w = fade(fz);
+	const float dv = GRAD ? dfade(fy) : 0.f, dw = GRAD ? dfade(fz) : 0.f;
+	// y/z corners c = by + 2 bz
+	const float Wyz[4] = {(1.f - v) * (1.f - w), v * (1.f - w), (1.f - v) * w, v * w};
+	const float dWy[4] = {-dv * (1.f - w), dv * (1.f - w), -dv * w, dv * w};
+	const float dWz[4] = {-(1.f - v) * dw, -v * dw, (1.f - v) * dw, v * dw};
+	const uint32_t y0 = (uint32_t)iy * HY, z0 = ((uint32_t)iz * HZ) ^ key, z1 = ((uint32_t)iz * HZ + HZ) ^ key;
+	const uint32_t yz[4] = {y0 ^ z0, (y0 + HY) ^ z0, y0 ^ z1, (y0 + HY) ^ z1};
+	const float ys[4] = {fy, fy - 1.f, fy, fy - 1.f}, zs[4] = {fz, fz, fz - 1.f, fz - 1.f};
+	int r = 0;
+	#pragma unroll 1
+	while (r < R) { // one segment of samples sharing an x cell (the same for every lane)
+		const int cx = (int)floorf(rc.px(r) * f);
+		float GX[2], Cc[2], Py[2], Qy[2], Pz[2], Qz[2];
+		const uint32_t xh0 = (uint32_t)cx * HX;
+		#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			const uint32_t xh = xh0 + (h ? HX : 0u);
+			float gxs = 0.f, cs = 0.f, pys = 0.f, qys = 0.f, pzs = 0.f, qzs = 0.f;
+			#pragma unroll
+			for (int c = 0; c < 4; c++) {
+				const uint32_t hh = mix32(xh ^ yz[c]);
+				if (VALUE) {
+					const float val = hash_signed(hh);
+					cs += Wyz[c] * val;
+					if (GRAD) { qys += dWy[c] * val; qzs += dWz[c] * val; }
+				} else {
+					const V3f g = grad_vec(hh);
+					const float cyz = g.y * ys[c] + g.z * zs[c];
+					gxs += Wyz[c] * g.x;
+					cs += Wyz[c] * cyz;
+					if (GRAD) {
+						pys += dWy[c] * g.x;
+						qys += dWy[c] * cyz + Wyz[c] * g.y;
+						pzs += dWz[c] * g.x;
+						qzs += dWz[c] * cyz + Wyz[c] * g.z;
+					}
+				}
+			}
+			GX[h] = gxs; Cc[h] = cs; Py[h] = pys; Qy[h] = qys; Pz[h] = pzs; Qz[h] = qzs;
+		}
+		#pragma unroll 1
+		for (; r < R; r++) {
+			const float qx = rc.px(r) * f;
+			const float fx0 = floorf(qx);
+			if ((int)fx0 != cx) break;
+			const float fx = qx - fx0;
+			const float u = fade(fx);
+			const float A0 = VALUE ? Cc[0] : fx * GX[0] + Cc[0];
+			const float A1 = VALUE ? Cc[1] : (fx - 1.f) * GX[1] + Cc[1];
+			const float dA = A1 - A0;
+			const float n = A0 + u * dA;
+			float s = n, ds = 1.f;
+			if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
+			if (GRAD) {
+				const float du = dfade(fx);
+				const float dnx = (VALUE ? 0.f : GX[0] + u * (GX[1] - GX[0])) + du * dA;
+				const float y0v = VALUE ? Qy[0] : fx * Py[0] + Qy[0], y1v = VALUE ? Qy[1] : (fx - 1.f) * Py[1] + Qy[1];
+				const float z0v = VALUE ? Qz[0] : fx * Pz[0] + Qz[0], z1v = VALUE ? Qz[1] : (fx - 1.f) * Pz[1] + Qz[1];
+				const float k = -amp * ds * f;
+				acc_add(acc, r * stride, -amp * s, k * dnx, k * (y0v + u * (y1v - y0v)), k * (z0v + u * (z1v - z0v)));
+			} else {
+				acc_add(acc, r * stride, -amp * s, 0.f, 0.f, 0.f);
+			}
+		}
+	}
+}
+
+// cellular noise (one octave) over samples [r0, r0 + CELL_SUB); DIST/OP fixed
+// at compile time. Returns false (nothing accumulated) when the sub-run spans
+// more than two x cells; the caller then evaluates those samples one by one.
+template<bool GRAD, int DIST, int OP>
+UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
+	constexpr int S = CELL_SUB;
+	const float qy = rc.py * f, qz = rc.pz * f;
+	const float fy0 = floorf(qy), fz0 = floorf(qz);
+	const int iy = (int)fy0, iz = (int)fz0;
+	const float fy = qy - fy0, fz = qz - fz0;
+	int ixr[S];
+	float fxr[S];
+	#pragma unroll
+	for (int r = 0; r < S; r++) {
+		const float qx = rc.px(r0 + r) * f;
+		const float fx0 = floorf(qx);
+		ixr[r] = (int)fx0;
+		fxr[r] = qx - fx0;
+	}
+	const int ixa = ixr[0], ixb = ixr[S - 1];
+	if (ixb - ixa > 1) return false;
+	float F1[S], F2[S];
+	int I1[S], I2[S]; // candidate ids: (column offset from ixa - 1) * 9 + (dy + 1) * 3 + (dz + 1)
+	#pragma unroll
+	for (int r = 0; r < S; r++) { F1[r] = 1e20f; F2[r] = 1e20f; I1[r] = 0; I2[r] = 0; }
+	const int ncol = ixb - ixa + 3;
+	#pragma unroll 1
+	for (int col = 0; col < ncol; col++) {
+		const int cxi = ixa - 1 + col;
+		const uint32_t xh = (uint32_t)cxi * HX;
+		#pragma unroll 1
+		for (int yz = 0; yz < 9; yz++) {
+			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
+			const uint32_t h = mix32(xh ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
+			const float vy = ((float)dy + jitter(h, 10)) - fy;
+			const float vz = ((float)dz + jitter(h, 20)) - fz;
+			const float jx = jitter(h, 0);
+			const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
+			const int id = col * 9 + yz;
+			#pragma unroll
+			for (int r = 0; r < S; r++) {
+				// the candidate column must lie in this sample's 3x3x3 neighbourhood
+				const bool ok = cxi >= ixr[r] - 1 && cxi <= ixr[r] + 1;
+				const float vx = ((float)(cxi - ixr[r]) + jx) - fxr[r];
+				float d;
+				if (DIST == 0) d = vx * vx + e2yz;
+				else if (DIST == 1) d = fabsf(vx) + m1yz;
+				else d = (vx * vx + e2yz) + (fabsf(vx) + m1yz);
+				d = ok ? d : 1e20f;
+				const bool b1 = d < F1[r], b2 = d < F2[r];
+				F2[r] = b1 ? F1[r] : (b2 ? d : F2[r]);
+				if (GRAD || OP == 0) I2[r] = b1 ? I1[r] : (b2 ? id : I2[r]);
+				F1[r] = b1 ? d : F1[r];
+				if (GRAD || OP == 0) I1[r] = b1 ? id : I1[r];
+			}
+		}
+	}
+	#pragma unroll
+	for (int r = 0; r < S; r++) {
+		float a = F1[r], b = F2[r];
+		if (DIST == 0) { a = sqrtf(a); b = sqrtf(b); }
+		V3f v1 = zero3(), v2 = zero3();
+		uint32_t h1 = 0;
+		if (GRAD || OP == 0) {
+			// rebuild the winners' difference vectors (q - p) from their ids
+			#pragma unroll
+			for (int wsel = 0; wsel < 2; wsel++) {
+				const int id = wsel ? I2[r] : I1[r];
+				const int col = id / 9, yz = id % 9;
+				const int cxi = ixa - 1 + col, dy = yz / 3 - 1, dz = yz % 3 - 1;
+				const uint32_t h = mix32(((uint32_t)cxi * HX) ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
+				const V3f vv = v3(((float)(cxi - ixr[r]) + jitter(h, 0)) - fxr[r], ((float)dy + jitter(h, 10)) - fy, ((float)dz + jitter(h, 20)) - fz);
+				if (wsel) v2 = vv;
+				else { v1 = vv; h1 = h; }
+			}
+		}
+		V3f dF1 = zero3(), dF2 = zero3();
+		if (GRAD) { dF1 = cell_dist_grad(v1, a, DIST); dF2 = cell_dist_grad(v2, b, DIST); }
+		float n;
+		V3f dn;
+		switch (OP) {
+			case 0: n = hash_signed(mix32(h1)); dn = zero3(); break;
+			case 1: n = a - 1.f; dn = dF1; break;
+			case 2: n = b - 1.f; dn = dF2; break;
+			case 3: n = (a + b) * 0.5f - 1.f; dn = (dF1 + dF2) * 0.5f; break;
+			case 4: n = b - a - 1.f; dn = dF2 - dF1; break;
+			case 5: n = a * b * 0.5f - 1.f; dn = (dF1 * b + dF2 * a) * 0.5f; break;
+			default: n = a / b - 1.f; dn = (dF1 * b - dF2 * a) * (1.f / (b * b)); break;
+		}
+		float s = n, ds = 1.f;
+		if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
+		if (GRAD) {
+			const float k = -amp * ds * f;
+			acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
+		} else {
+			acc_add(acc, (r0 + r) * stride, -amp * s, 0.f, 0.f, 0.f);
+		}
+	}
+	return true;
+}
+
+// a layer over a run: TYPE 0 value, 2 Perlin, cellular spec (see cell_spec)
+template<bool GRAD, int TYPE>
+UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride) {
+	const bool ridged = L.fractal == UP_FRACTAL_RIDGED;
+	#pragma unroll 1
+	for (int i = 0; i < L.octaves; i++) {
+		const float f = L.freq[i], a = L.amp[i];
+		const uint32_t key = seed_key(L.seed + (uint32_t)i);
+		if (TYPE == 0) lattice_octave_run<GRAD, true>(rc, R, f, a, ridged, key, acc, stride);
+		else if (TYPE == 2) lattice_octave_run<GRAD, false>(rc, R, f, a, ridged, key, acc, stride);
+		else {
+			constexpr int DIST = ((TYPE >> 4) & 15) - 1, OP = ((TYPE >> 8) & 15) - 1;
+			#pragma unroll 1
+			for (int r0 = 0; r0 < R; r0 += CELL_SUB) {
+				if (cellular_subrun<GRAD, DIST, OP>(rc, r0, f, a, ridged, key, acc, stride)) continue;
+				#pragma unroll 1
+				for (int r = r0; r < r0 + CELL_SUB; r++) {
+					const NG n = cellular_n<GRAD, DIST, OP>(v3(rc.px(r) * f, rc.py * f, rc.pz * f), key, DIST, OP);
+					float s = n.v, ds = 1.f;
+					if (ridged) { s = 1.f - 2.f * fabsf(n.v); ds = n.v > 0.f ? -2.f : (n.v < 0.f ? 2.f : 0.f); }
+					const float k = -a * ds * f;
+					acc_add(acc, r * stride, -a * s, k * n.g.x, k * n.g.y, k * n.g.z);
+				}
+			}
+		}
+	}
+}
+
+// one run: base shape plus layers into acc (R must be a multiple of CELL_SUB)
+template<bool GRAD, int T0, int T1>
+UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride) {
+	#pragma unroll 1
+	for (int r = 0; r < R; r++) {
+		const NG b = synth_base<GRAD>(P, v3(rc.px(r), rc.py, rc.pz));
+		acc_set(acc, r * stride, b.v, b.g.x, b.g.y, b.g.z);
+	}
+	if (P.n_layers > 0) layer_run<GRAD, T0>(P.layer[0], rc, R, acc, stride);
+	if (P.n_layers > 1) layer_run<GRAD, T1>(P.layer[1], rc, R, acc, stride);
+}
+
+} // namespace up

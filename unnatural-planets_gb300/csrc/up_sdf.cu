@@ -9,6 +9,7 @@
 // writes to x-fastest planes.
 #include "up_internal.h"
 #include "up_synth.cuh"
+#include "up_grid_runs.cuh"
 
 #include <mutex>
 
@@ -58,6 +59,79 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
 }
 
+// x-coherent runs (up_grid_runs.cuh): a warp task is RUN_R consecutive x
+// samples of 32 rows; accumulators in dynamic shared memory, RUNS_T slots
+// per sample index, so thread t owns acc[r * RUNS_T + t]
+constexpr int RUNS_T = 128;
+template<bool GRAD, int T0, int T1>
+__global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
+	float *__restrict__ grad, unsigned *__restrict__ nanflag) {
+	typedef typename AccOf<GRAD>::T A;
+	extern __shared__ __align__(16) unsigned char runs_smem[];
+	A *acc = (A *)runs_smem + threadIdx.x;
+	constexpr int R = RUN_R;
+	const uint32_t nx = g.n[0], ny = g.n[1];
+	const uint32_t nrows = ny * g.n[2];
+	const uint32_t nruns = (nx + R - 1) / R;
+	const uint64_t ntasks = (uint64_t)nruns * ((nrows + 31) / 32);
+	const uint64_t plane = (uint64_t)nx * nrows;
+	const uint32_t lane = threadIdx.x & 31;
+	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	RunCtx rc;
+	rc.lo_x = g.lo[0];
+	rc.step_x = g.step[0];
+	rc.nx = nx;
+	bool bad = false;
+	for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nwarps) {
+		const uint32_t run = (uint32_t)(t % nruns), grp = (uint32_t)(t / nruns);
+		const uint32_t row_raw = grp * 32 + lane;
+		const bool live = row_raw < nrows;
+		const uint32_t row = live ? row_raw : nrows - 1;
+		const uint32_t j = row % ny, k = row / ny;
+		rc.i0 = run * R;
+		rc.py = grid_coord(g, 1, j);
+		rc.pz = grid_coord(g, 2, k);
+		synth_run<GRAD, T0, T1>(P, rc, R, acc, RUNS_T);
+		if (!live) continue;
+		const uint64_t base = (uint64_t)row * nx + rc.i0;
+		const bool vec = rc.i0 + R <= nx && (base & 3) == 0;
+		#pragma unroll 1
+		for (int r = 0; r < R; r += 4) {
+			float v[4], gx[4], gy[4], gz[4];
+			#pragma unroll
+			for (int q = 0; q < 4; q++) {
+				if (GRAD) {
+					const Acc4 x = ((const Acc4 *)acc)[(r + q) * RUNS_T];
+					v[q] = x.v; gx[q] = x.gx; gy[q] = x.gy; gz[q] = x.gz;
+				} else {
+					v[q] = ((const float *)acc)[(r + q) * RUNS_T];
+				}
+				bad |= isnan(v[q]);
+			}
+			if (vec) {
+				*(float4 *)(out + base + r) = make_float4(v[0], v[1], v[2], v[3]);
+				if (GRAD) {
+					*(float4 *)(grad + base + r) = make_float4(gx[0], gx[1], gx[2], gx[3]);
+					*(float4 *)(grad + plane + base + r) = make_float4(gy[0], gy[1], gy[2], gy[3]);
+					*(float4 *)(grad + 2 * plane + base + r) = make_float4(gz[0], gz[1], gz[2], gz[3]);
+				}
+			} else {
+				#pragma unroll
+				for (int q = 0; q < 4; q++)
+					if (rc.i0 + r + q < nx) {
+						out[base + r + q] = v[q];
+						if (GRAD) {
+							grad[base + r + q] = gx[q];
+							grad[plane + base + r + q] = gy[q];
+							grad[2 * plane + base + r + q] = gz[q];
+						}
+					}
+			}
+		}
+	}
+	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
+}
+
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(256) synth_points_kernel(const up_synth_program P, const float *__restrict__ xyz, uint64_t n,
 	float *__restrict__ out, float *__restrict__ grad, unsigned *__restrict__ nanflag) {
@@ -98,10 +172,27 @@ static cudaError_t launch_persistent(K kernel, uint64_t work, cudaStream_t s, A.
 	return cudaGetLastError();
 }
 
+template<bool GRAD, class K, class... A>
+static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, A... args) {
+	// 32 KiB (value + gradient) or 8 KiB: below the 48 KiB default limit
+	constexpr size_t smem = (size_t)RUN_R * RUNS_T * sizeof(typename AccOf<GRAD>::T);
+	static_assert(smem <= 48 * 1024, "runs accumulators exceed the default shared-memory limit");
+	uint64_t blocks = (uint64_t)persistent_blocks((const void *)kernel, RUNS_T, smem);
+	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] * g.n[2] + 31) / 32);
+	const uint64_t need = (tasks + RUNS_T / 32 - 1) / (RUNS_T / 32);
+	if (blocks > need) blocks = need > 0 ? need : 1;
+	kernel<<<(unsigned)blocks, RUNS_T, smem, s>>>(args...);
+	return cudaGetLastError();
+}
+
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s) {
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
 	const Spec sp = spec_of(P);
+	if (sp == SPEC_PERLIN_CELL) {
+		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag);
+		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag);
+	}
 	if (grad) {
 		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag);
 		if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<true, 3, -1>, n, s, P, g, out, grad, nanflag);
