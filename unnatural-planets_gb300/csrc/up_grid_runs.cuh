@@ -8,9 +8,10 @@
 // every code block appears once (the unrolled form overflowed the
 // instruction cache).
 // Lattice noise (value, Perlin): per octave, the y/z fade weights are formed
-// once per run; the 8 corner hashes and gradients are formed only when the
-// x cell changes (once per segment of samples sharing a cell) and folded
-// into 12 coefficients (x halves h = 0/1 of
+// once per run; corner hashes and gradients are formed only when the x cell
+// changes (once per segment of samples sharing a cell; 4 of the 8 corners
+// when the new cell is the next one along x, whose low face is the old high
+// face) and folded into 12 coefficients (x halves h = 0/1 of
 //   A_h(t) = t GX_h + C_h,  dA_h/dy = t P_hy + Q_hy,  dA_h/dz = t P_hz + Q_hz),
 // after which a sample's value and analytic gradient cost a few FMAs:
 //   n = A0(fx) + u (A1(fx - 1) - A0(fx)),
@@ -19,10 +20,13 @@
 // Cellular noise: in sub-runs of 8 samples, candidates outer and samples
 // inner -- each of the 3 or 4 x columns of 9 candidate cells is hashed once
 // per sub-run, a sample ignores columns outside its own 3x3x3 neighbourhood
-// (so results equal the per-sample search); F1/F2 are tracked by squared
-// length and candidate id, and the winners' difference vectors are rebuilt
-// for the gradient.
-// Results equal the per-sample kernels up to FP32 reassociation.
+// (so the candidate set equals the per-sample search). The two nearest are
+// kept as integer keys (distance bits with the candidate id in the low 6
+// mantissa bits), and the winners' exact distances and difference vectors
+// are rebuilt from the ids. Values equal the per-sample kernels up to FP32
+// reassociation; the key's 2^-17 relative quantisation can only reorder
+// candidates whose distances agree to that level (F1/F2 near-ties, where
+// the gradient of F2 - F1 is discontinuous anyway).
 #pragma once
 #include "up_synth.cuh"
 
@@ -46,6 +50,29 @@ struct RunCtx {
 #endif
 	}
 };
+
+// Perlin gradient vectors (grad_vec of h & 15) in shared memory: a lookup is
+// one shared load instead of a chain of integer selects on the ALU pipe.
+// runs_tables_init() fills it at the start of every kernel that calls
+// synth_run (host builds compute grad_vec directly).
+#ifdef __CUDACC__
+__shared__ float4 g_runs_gradtab[16];
+__device__ __forceinline__ void runs_tables_init() {
+	if (threadIdx.x < 16) {
+		const V3f v = grad_vec(threadIdx.x);
+		g_runs_gradtab[threadIdx.x] = make_float4(v.x, v.y, v.z, 0.f);
+	}
+	__syncthreads();
+}
+#endif
+UP_HD V3f grad_lookup(uint32_t h) {
+#ifdef __CUDA_ARCH__
+	const float4 t = g_runs_gradtab[h & 15u];
+	return v3(t.x, t.y, t.z);
+#else
+	return grad_vec(h);
+#endif
+}
 
 // per-sample accumulator: value and gradient (Acc4) or value only (float);
 // acc[r * stride] belongs to sample r
@@ -78,15 +105,21 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 	const uint32_t y0 = (uint32_t)iy * HY, z0 = ((uint32_t)iz * HZ) ^ key, z1 = ((uint32_t)iz * HZ + HZ) ^ key;
 	const uint32_t yz[4] = {y0 ^ z0, (y0 + HY) ^ z0, y0 ^ z1, (y0 + HY) ^ z1};
 	const float ys[4] = {fy, fy - 1.f, fy, fy - 1.f}, zs[4] = {fz, fz, fz - 1.f, fz - 1.f};
+	// coefficients of the two x faces of the current cell; when the next
+	// segment is the neighbouring cell, its low face is the old high face
+	float GX[2], Cc[2], Py[2], Qy[2], Pz[2], Qz[2];
+	int cx_prev = 0;
 	int r = 0;
 	#pragma unroll 1
 	while (r < R) { // one segment of samples sharing an x cell (the same for every lane)
 		const int cx = (int)floorf(rc.px(r) * f);
-		float GX[2], Cc[2], Py[2], Qy[2], Pz[2], Qz[2];
-		const uint32_t xh0 = (uint32_t)cx * HX;
+		const bool carry = r > 0 && cx == cx_prev + 1;
+		cx_prev = cx;
+		if (carry) { GX[0] = GX[1]; Cc[0] = Cc[1]; Py[0] = Py[1]; Qy[0] = Qy[1]; Pz[0] = Pz[1]; Qz[0] = Qz[1]; }
 		#pragma unroll
 		for (int h = 0; h < 2; h++) {
-			const uint32_t xh = xh0 + (h ? HX : 0u);
+			if (h == 0 && carry) continue;
+			const uint32_t xh = (uint32_t)(cx + h) * HX;
 			float gxs = 0.f, cs = 0.f, pys = 0.f, qys = 0.f, pzs = 0.f, qzs = 0.f;
 			#pragma unroll
 			for (int c = 0; c < 4; c++) {
@@ -96,7 +129,7 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 					cs += Wyz[c] * val;
 					if (GRAD) { qys += dWy[c] * val; qzs += dWz[c] * val; }
 				} else {
-					const V3f g = grad_vec(hh);
+					const V3f g = grad_lookup(hh);
 					const float cyz = g.y * ys[c] + g.z * zs[c];
 					gxs += Wyz[c] * g.x;
 					cs += Wyz[c] * cyz;
@@ -140,6 +173,18 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 // cellular noise (one octave) over samples [r0, r0 + CELL_SUB); DIST/OP fixed
 // at compile time. Returns false (nothing accumulated) when the sub-run spans
 // more than two x cells; the caller then evaluates those samples one by one.
+// The x cells are the same for every lane. A candidate is ranked by its
+// distance with the low 6 mantissa bits replaced by its id (column * 9 + yz):
+// the two smallest keys per sample are kept with integer min/max, and the
+// winners' exact distances and difference vectors are rebuilt from the ids.
+UP_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
+UP_HD uint32_t umax32(uint32_t a, uint32_t b) { return a > b ? a : b; }
+template<int DIST>
+UP_HD float cell_metric(float vx, float e2yz, float m1yz) {
+	if (DIST == 0) return vx * vx + e2yz;
+	if (DIST == 1) return fabsf(vx) + m1yz;
+	return (vx * vx + e2yz) + (fabsf(vx) + m1yz);
+}
 template<bool GRAD, int DIST, int OP>
 UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
 	constexpr int S = CELL_SUB;
@@ -147,74 +192,76 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 	const float fy0 = floorf(qy), fz0 = floorf(qz);
 	const int iy = (int)fy0, iz = (int)fz0;
 	const float fy = qy - fy0, fz = qz - fz0;
-	int ixr[S];
-	float fxr[S];
+	const int ixa = (int)floorf(rc.px(r0) * f);
+	const int ixb = (int)floorf(rc.px(r0 + S - 1) * f);
+	if (ixb - ixa > 1) return false;
+	// sx[r] = (ix_r - ixa) + fx_r: then x difference to a candidate in column
+	// cxi = ixa - 1 + col is ((col - 1) + jitter) - sx[r]
+	float sx[S];
+	int split = S; // samples [0, split) are in cell ixa, the rest in ixa + 1
 	#pragma unroll
-	for (int r = 0; r < S; r++) {
+	for (int r = S - 1; r >= 0; r--) {
 		const float qx = rc.px(r0 + r) * f;
 		const float fx0 = floorf(qx);
-		ixr[r] = (int)fx0;
-		fxr[r] = qx - fx0;
+		const bool second = (int)fx0 != ixa;
+		sx[r] = second ? 1.f + (qx - fx0) : qx - fx0;
+		if (second) split = r;
 	}
-	const int ixa = ixr[0], ixb = ixr[S - 1];
-	if (ixb - ixa > 1) return false;
-	float F1[S], F2[S];
-	int I1[S], I2[S]; // candidate ids: (column offset from ixa - 1) * 9 + (dy + 1) * 3 + (dz + 1)
+	uint32_t K1[S], K2[S];
 	#pragma unroll
-	for (int r = 0; r < S; r++) { F1[r] = 1e20f; F2[r] = 1e20f; I1[r] = 0; I2[r] = 0; }
+	for (int r = 0; r < S; r++) { K1[r] = 0xFFFFFFFFu; K2[r] = 0xFFFFFFFFu; }
 	const int ncol = ixb - ixa + 3;
 	#pragma unroll 1
 	for (int col = 0; col < ncol; col++) {
-		const int cxi = ixa - 1 + col;
-		const uint32_t xh = (uint32_t)cxi * HX;
+		const uint32_t xh = (uint32_t)(ixa - 1 + col) * HX;
+		// a column outside a sample's 3x3x3 neighbourhood is pushed far away
+		float sc[S];
+		#pragma unroll
+		for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
+		const float fcol = (float)(col - 1);
 		#pragma unroll 1
 		for (int yz = 0; yz < 9; yz++) {
 			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
 			const uint32_t h = mix32(xh ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
 			const float vy = ((float)dy + jitter(h, 10)) - fy;
 			const float vz = ((float)dz + jitter(h, 20)) - fz;
-			const float jx = jitter(h, 0);
+			const float T = fcol + jitter(h, 0);
 			const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
-			const int id = col * 9 + yz;
+			const uint32_t id = (uint32_t)(col * 9 + yz);
 			#pragma unroll
 			for (int r = 0; r < S; r++) {
-				// the candidate column must lie in this sample's 3x3x3 neighbourhood
-				const bool ok = cxi >= ixr[r] - 1 && cxi <= ixr[r] + 1;
-				const float vx = ((float)(cxi - ixr[r]) + jx) - fxr[r];
-				float d;
-				if (DIST == 0) d = vx * vx + e2yz;
-				else if (DIST == 1) d = fabsf(vx) + m1yz;
-				else d = (vx * vx + e2yz) + (fabsf(vx) + m1yz);
-				d = ok ? d : 1e20f;
-				const bool b1 = d < F1[r], b2 = d < F2[r];
-				F2[r] = b1 ? F1[r] : (b2 ? d : F2[r]);
-				if (GRAD || OP == 0) I2[r] = b1 ? I1[r] : (b2 ? id : I2[r]);
-				F1[r] = b1 ? d : F1[r];
-				if (GRAD || OP == 0) I1[r] = b1 ? id : I1[r];
+				const uint32_t k = (f_bits(cell_metric<DIST>(T - sc[r], e2yz, m1yz)) & ~63u) | id;
+				K2[r] = umin32(K2[r], umax32(K1[r], k));
+				K1[r] = umin32(K1[r], k);
 			}
 		}
 	}
-	#pragma unroll
+	#pragma unroll 1
 	for (int r = 0; r < S; r++) {
-		float a = F1[r], b = F2[r];
-		if (DIST == 0) { a = sqrtf(a); b = sqrtf(b); }
-		V3f v1 = zero3(), v2 = zero3();
+		float Fw[2];
+		V3f vw[2], dFw[2] = {zero3(), zero3()};
 		uint32_t h1 = 0;
-		if (GRAD || OP == 0) {
-			// rebuild the winners' difference vectors (q - p) from their ids
-			#pragma unroll
-			for (int wsel = 0; wsel < 2; wsel++) {
-				const int id = wsel ? I2[r] : I1[r];
-				const int col = id / 9, yz = id % 9;
-				const int cxi = ixa - 1 + col, dy = yz / 3 - 1, dz = yz % 3 - 1;
-				const uint32_t h = mix32(((uint32_t)cxi * HX) ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
-				const V3f vv = v3(((float)(cxi - ixr[r]) + jitter(h, 0)) - fxr[r], ((float)dy + jitter(h, 10)) - fy, ((float)dz + jitter(h, 20)) - fz);
-				if (wsel) v2 = vv;
-				else { v1 = vv; h1 = h; }
+		#pragma unroll
+		for (int wsel = 0; wsel < 2; wsel++) {
+			const uint32_t id = (wsel ? K2[r] : K1[r]) & 63u;
+			const int col = (int)(id / 9u), yz = (int)(id % 9u);
+			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
+			const uint32_t h = mix32(((uint32_t)(ixa - 1 + col) * HX) ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
+			const float vy = ((float)dy + jitter(h, 10)) - fy;
+			const float vz = ((float)dz + jitter(h, 20)) - fz;
+			const float vx = ((float)(col - 1) + jitter(h, 0)) - sx[r];
+			const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
+			Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
+			vw[wsel] = v3(vx, vy, vz);
+			if (GRAD) {
+				// d F / d p for v = q - p (dv/dp = -I); Euclidean: -v / |v|
+				if (DIST == 0) dFw[wsel] = d > 0.f ? vw[wsel] * -rsqrt_hd(d) : zero3();
+				else dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
 			}
+			if (!wsel) h1 = h;
 		}
-		V3f dF1 = zero3(), dF2 = zero3();
-		if (GRAD) { dF1 = cell_dist_grad(v1, a, DIST); dF2 = cell_dist_grad(v2, b, DIST); }
+		const float a = Fw[0], b = Fw[1];
+		const V3f dF1 = dFw[0], dF2 = dFw[1];
 		float n;
 		V3f dn;
 		switch (OP) {
@@ -228,12 +275,8 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		}
 		float s = n, ds = 1.f;
 		if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
-		if (GRAD) {
-			const float k = -amp * ds * f;
-			acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
-		} else {
-			acc_add(acc, (r0 + r) * stride, -amp * s, 0.f, 0.f, 0.f);
-		}
+		const float k = -amp * ds * f;
+		acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
 	}
 	return true;
 }

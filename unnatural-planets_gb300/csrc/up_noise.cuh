@@ -21,6 +21,7 @@
 #pragma once
 #include <stdint.h>
 #include <math.h>
+#include <string.h>
 
 #ifdef __CUDACC__
 #define UP_HD __host__ __device__ __forceinline__
@@ -31,6 +32,36 @@
 #endif
 
 namespace up {
+
+// float <-> bits
+UP_HD uint32_t f_bits(float x) {
+#ifdef __CUDA_ARCH__
+	return __float_as_uint(x);
+#else
+	uint32_t u;
+	memcpy(&u, &x, 4);
+	return u;
+#endif
+}
+UP_HD float bits_f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+	return __uint_as_float(u);
+#else
+	float x;
+	memcpy(&x, &u, 4);
+	return x;
+#endif
+}
+
+// reciprocal square root: the hardware approximation on the device (a few
+// ulp), correctly rounded 1 / sqrt on the host; used for unit vectors only
+UP_HD float rsqrt_hd(float x) {
+#ifdef __CUDA_ARCH__
+	return rsqrtf(x);
+#else
+	return 1.f / sqrtf(x);
+#endif
+}
 
 struct V3f { float x, y, z; };
 UP_HD V3f v3(float x, float y, float z) { V3f r; r.x = x; r.y = y; r.z = z; return r; }
@@ -263,7 +294,11 @@ UP_HD NG simplex_n(V3f p, uint32_t key) {
 }
 
 // ---------------------------------------------------------------- cellular
-UP_HD float jitter(uint32_t h, int s) { return (float)((h >> s) & 1023U) * (1.0f / 1024.0f) + (1.0f / 2048.0f); }
+// (m + 1/2) / 1024 for the 10-bit field m = (h >> s) & 1023: the float
+// 1 + m / 1024 is assembled in the mantissa and 1 - 1/2048 subtracted, which
+// is exact (both in [1, 2)), so this equals m * (1/1024) + 1/2048 without an
+// integer-to-float conversion
+UP_HD float jitter(uint32_t h, int s) { return bits_f(0x3F800000u | (((h >> s) & 1023U) << 13)) - 0.99951171875f; }
 
 UP_HD float signf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
 // gradient with respect to p of the distance metric of v = q - p

@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 	const uint64_t plane = (uint64_t)nx * nrows;
 	const uint32_t lane = threadIdx.x & 31;
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	runs_tables_init();
 	RunCtx rc;
 	rc.lo_x = g.lo[0];
 	rc.step_x = g.step[0];

@@ -98,7 +98,15 @@ UP_HD NG synth_base(const up_synth_program &P, V3f p) {
 			const float ik = 1.f / P.k;
 			#pragma unroll 1
 			for (int s = 0; s < P.n_spheres; s++) {
-				const NG sd = sphere_d(p, v3(P.sphere[s][0], P.sphere[s][1], P.sphere[s][2]), P.sphere[s][3]);
+				const V3f c = v3(P.sphere[s][0], P.sphere[s][1], P.sphere[s][2]);
+				// A sphere at distance l >= radius + b + k leaves the blend
+				// weight saturated (h = 1): the smooth minimum returns b and
+				// its gradient unchanged, so such spheres are skipped (the
+				// margin keeps h exactly 1 under FP32 rounding).
+				const V3f dc = p - c;
+				const float lim = P.sphere[s][3] + b.v + P.k * 1.001f + 1e-6f;
+				if (lim <= 0.f || dot(dc, dc) >= lim * lim) continue;
+				const NG sd = sphere_d(p, c, P.sphere[s][3]);
 				const SMin m = smooth_min_d(b.v, sd.v, P.k, ik);
 				b = ng(m.s, b.g * m.da + sd.g * m.db);
 			}
