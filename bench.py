@@ -272,7 +272,7 @@ def run_ours(args) -> None:
                    "l2": "no inputs; 2.1 GB of outputs per step (> 129 MB L2)"},
         "plain_gsamples_s": ws * N / (t_plain * 1e-3) / 1e9, "plain_ms": t_plain,
         "ms_per_planet": sum(planet_ms) / len(planet_ms),
-        "planet": {"what": f"{args.grid}^3 value sampling + dual contouring (count, emit, Hermite, FP64 QEF, quads) into device buffers",
+        "planet": {"what": f"{args.grid}^3 value sampling + dual contouring (count, scan, emit, Hermite, QEF (FP32; FP64 near the truncation threshold), quads) into device buffers",
                    "vertices": V, "triangles": I // 3},
         "e2e": {"value": ws * N / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 * N,
                 "what": "up_sdf_grid value+gradient into pinned host buffers"},

@@ -223,8 +223,9 @@ int up_sdf_grid(up_context *ctx, uint32_t fields_mask, const up_grid *grid, floa
  * (meshGeneration.cpp:40) and the flow of meshGenerateGeneric (:32-44).
  * Samples the field on grid (or takes it from values when not NULL: a
  * host or device array of nx*ny*nz floats), finds sign-change edges, places
- * one vertex per active cell by an FP64 QEF solve on analytic Hermite
- * normals, and emits two triangles per interior sign-change edge, wound so
+ * one vertex per active cell by a QEF solve on analytic Hermite normals
+ * (FP32; FP64 for cells whose eigenvalue truncation is within FP32
+ * rounding of the threshold), and emits two triangles per interior sign-change edge, wound so
  * that normals point to increasing field values (outwards). Vertex order is
  * the linear cell order; triangle order is (grid point, axis) order.
  * When capacities are too small returns UP_ERR_CAPACITY with the required

@@ -406,7 +406,7 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 		}
 		DcScratch S;
 		const uint32_t nb = dc_num_blocks(g);
-		S.blk_counts = (uint32_t *)buf(ctx, B_DC_BLK, (size_t)nb * 12);
+		S.blk_counts = (uint32_t *)buf(ctx, B_DC_BLK, dc_scan_words(nb) * 4);
 		S.totals = (uint32_t *)buf(ctx, B_DC_TOT, 16);
 		S.cell_map = (uint32_t *)buf(ctx, B_DC_CMAP, nc * 4);
 		S.edge_map = (uint32_t *)buf(ctx, B_DC_EMAP, np * 12);

@@ -204,7 +204,6 @@ __global__ void __launch_bounds__(256) batch_quads_kernel(const BatchChunkDev *_
 }
 
 // ---------------------------------------------------------------- host side
-void dc_scan_blocks(uint32_t *blk, uint32_t nb, uint32_t *totals, cudaStream_t s);
 
 struct DevBuf {
 	void *p = nullptr;
@@ -349,7 +348,7 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = S->tiles.ensure(nchunks * 4)) != cudaSuccess) return e;
 		if ((e = S->blkst.ensure(nchunks * 4)) != cudaSuccess) return e;
 		if ((e = S->grid.ensure(pts * 4)) != cudaSuccess) return e;
-		if ((e = S->blk.ensure(nb * 12)) != cudaSuccess) return e;
+		if ((e = S->blk.ensure(dc_scan_words((uint32_t)nb) * 4)) != cudaSuccess) return e;
 		if ((e = S->totals.ensure(16)) != cudaSuccess) return e;
 		if ((e = S->off.ensure((nchunks + 1) * 12)) != cudaSuccess) return e;
 		if ((e = S->cmap.ensure(cells * 4)) != cudaSuccess) return e;

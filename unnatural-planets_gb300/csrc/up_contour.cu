@@ -25,25 +25,54 @@ __global__ void __launch_bounds__(DC_T) dc_count_kernel(const float *__restrict_
 	}
 }
 
-// one block of 1024 threads: exclusive scan of the three block-count arrays
-// in place; totals[a] = sum
-__global__ void __launch_bounds__(1024) dc_scan_kernel(uint32_t *__restrict__ blk, uint32_t nblocks, uint32_t *__restrict__ totals) {
-	const uint32_t per = (nblocks + 1023) / 1024;
+// Exclusive scan of the three block-count arrays blk[a * nb + b] in place,
+// totals[a] = sum, in three launches: chunks of 1024 entries scanned by one
+// block each (coalesced), the chunk sums scanned by one block, the chunk
+// offsets added. The chunk sums live after the arrays: part = blk + 3 nb.
+__global__ void __launch_bounds__(1024) dc_scan_chunks_kernel(uint32_t *__restrict__ blk, uint32_t nb, uint32_t nch, uint32_t *__restrict__ part) {
+	const uint32_t x = blockIdx.x * 1024 + threadIdx.x;
 	for (int a = 0; a < 3; a++) {
-		uint32_t *arr = blk + (uint64_t)a * nblocks;
+		uint32_t *arr = blk + (uint64_t)a * nb;
+		const uint32_t v = x < nb ? arr[x] : 0u;
+		uint64_t tot;
+		const uint64_t ex = block_exscan<1024>(v, tot);
+		if (x < nb) arr[x] = (uint32_t)ex;
+		if (threadIdx.x == 0) part[a * nch + blockIdx.x] = (uint32_t)tot;
+	}
+}
+__global__ void __launch_bounds__(1024) dc_scan_top_kernel(uint32_t *__restrict__ part, uint32_t nch, uint32_t *__restrict__ totals) {
+	const uint32_t per = (nch + 1023) / 1024;
+	for (int a = 0; a < 3; a++) {
+		uint32_t *arr = part + (uint64_t)a * nch;
 		const uint32_t b0 = threadIdx.x * per;
 		uint64_t s = 0;
-		for (uint32_t b = b0; b < b0 + per && b < nblocks; b++) s += arr[b];
+		for (uint32_t b = b0; b < b0 + per && b < nch; b++) s += arr[b];
 		uint64_t tot;
 		uint64_t run = block_exscan<1024>(s, tot);
-		for (uint32_t b = b0; b < b0 + per && b < nblocks; b++) {
+		for (uint32_t b = b0; b < b0 + per && b < nch; b++) {
 			const uint32_t v = arr[b];
 			arr[b] = (uint32_t)run;
 			run += v;
 		}
 		if (threadIdx.x == 0) totals[a] = (uint32_t)tot;
-		__syncthreads();
 	}
+}
+__global__ void __launch_bounds__(1024) dc_scan_add_kernel(uint32_t *__restrict__ blk, uint32_t nb, uint32_t nch, const uint32_t *__restrict__ part) {
+	const uint32_t x = blockIdx.x * 1024 + threadIdx.x;
+	if (x >= nb) return;
+	#pragma unroll
+	for (int a = 0; a < 3; a++) blk[(uint64_t)a * nb + x] += part[a * nch + blockIdx.x];
+}
+
+size_t dc_scan_words(uint32_t nb) { return 3 * (size_t)nb + 3 * (size_t)((nb + 1023) / 1024); }
+
+cudaError_t dc_scan_blocks(uint32_t *blk, uint32_t nb, uint32_t *totals, cudaStream_t s) {
+	const uint32_t nch = (nb + 1023) / 1024;
+	uint32_t *part = blk + 3 * (size_t)nb;
+	if (nch) dc_scan_chunks_kernel<<<nch, 1024, 0, s>>>(blk, nb, nch, part);
+	dc_scan_top_kernel<<<1, 1024, 0, s>>>(part, nch, totals);
+	if (nch) dc_scan_add_kernel<<<nch, 1024, 0, s>>>(blk, nb, nch, part);
+	return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(DC_T) dc_emit_kernel(const float *__restrict__ d, const GridDev g, uint32_t npts, uint32_t nblocks,
@@ -107,11 +136,9 @@ cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_
 	dc_count_kernel<<<nb, DC_T, 0, s>>>(d, g, npts, nb, S.blk_counts);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
-	dc_scan_kernel<<<1, 1024, 0, s>>>(S.blk_counts, nb, S.totals);
-	return cudaGetLastError();
+	return dc_scan_blocks(S.blk_counts, nb, S.totals, s);
 }
 
-void dc_scan_blocks(uint32_t *blk, uint32_t nb, uint32_t *totals, cudaStream_t s) { dc_scan_kernel<<<1, 1024, 0, s>>>(blk, nb, totals); }
 
 cudaError_t dc_emit(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s) {
 	const uint32_t npts = g.n[0] * g.n[1] * g.n[2];

@@ -5,9 +5,11 @@
 //   inside(d) = d < 0; a cell is active when its 8 corner signs differ; a
 //   sign edge joins two samples of different sign; the Hermite point is
 //   x0 + t (x1 - x0), t = d0 / (d0 - d1) in FP64; the Hermite normal is the
-//   analytic gradient at that point; the cell vertex minimises the QEF in
-//   FP64 (cell-local units, mass-point centred, eight cyclic Jacobi sweeps,
-//   eigenvalues below 1e-2 of the largest truncated, clamped to the cell);
+//   analytic gradient at that point; the cell vertex minimises the QEF
+//   (cell-local units, mass-point centred, eight cyclic Jacobi sweeps,
+//   eigenvalues below 1e-2 of the largest truncated, clamped to the cell)
+//   in FP32, and in FP64 for the cells whose truncation decision lies
+//   within FP32 rounding;
 //   every sign edge with four cells emits two triangles wound outwards.
 // Pipeline: count (per 1024-point block: active cells, sign edges, quads) ->
 // exclusive scan of block counts -> emit (ordered lists and dense maps; order
@@ -172,10 +174,9 @@ __device__ __forceinline__ void dc_hermite_item(const E &ev, const float *__rest
 	n_out[2] = s.g.z * il;
 }
 
-// QEF vertex and normal of one active cell whose origin is grid point p
-template<class E>
-__device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
-	const uint32_t *__restrict__ edge_map, const double *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
+// FP64 QEF vertex (cell-local) of one active cell whose origin is grid point p
+static __device__ __noinline__ void dc_qef_vertex_fp64(const float *__restrict__ d, const GridDev &g, uint32_t p, const uint32_t *__restrict__ edge_map,
+	const double *__restrict__ edge_t, const float *__restrict__ edge_n, double v[3]) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t sxy = nx * ny;
 	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
@@ -214,9 +215,126 @@ __device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict
 			ne++;
 		}
 	}
-	double v[3];
 	dc_qef_solve(ne, pts, nms, v);
-	const V3f vp = v3((float)(o[0] + v[0] * st[0]), (float)(o[1] + v[1] * st[1]), (float)(o[2] + v[2] * st[2]));
+}
+
+// FP32 form of dc_qef_solve for the accumulated A = sum n n^T and
+// r = sum n (n . (p - m)) about the mass point m: the same eight cyclic
+// Jacobi sweeps and truncation rule. Returns false when an eigenvalue lies
+// within 1e-4 lmax of the truncation threshold 1e-2 lmax, or lmax is below
+// 1e-6 (FP32 rounding of the eigenvalues is ~1e-7 lmax, so every other
+// truncation decision equals the FP64 one); the caller then solves in FP64.
+__device__ __forceinline__ bool dc_qef_solve_f32(float a[3][3], const float r[3], const float m[3], float out[3]) {
+	float v[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+	#pragma unroll 1
+	for (int sweep = 0; sweep < 8; sweep++) {
+		#pragma unroll
+		for (int rr = 0; rr < 3; rr++) {
+			const int p = rr == 2 ? 1 : 0, q = rr == 0 ? 1 : 2;
+			const float apq = a[p][q];
+			if (fabsf(apq) < 1e-30f) continue;
+			const float theta = (a[q][q] - a[p][p]) / (2.f * apq);
+			const float t = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+			const float c = 1.f / sqrtf(t * t + 1.f), s = t * c;
+			#pragma unroll
+			for (int k = 0; k < 3; k++) {
+				const float akp = a[k][p], akq = a[k][q];
+				a[k][p] = c * akp - s * akq;
+				a[k][q] = s * akp + c * akq;
+			}
+			#pragma unroll
+			for (int k = 0; k < 3; k++) {
+				const float apk = a[p][k], aqk = a[q][k];
+				a[p][k] = c * apk - s * aqk;
+				a[q][k] = s * apk + c * aqk;
+			}
+			#pragma unroll
+			for (int k = 0; k < 3; k++) {
+				const float vkp = v[k][p], vkq = v[k][q];
+				v[k][p] = c * vkp - s * vkq;
+				v[k][q] = s * vkp + c * vkq;
+			}
+		}
+	}
+	const float lmax = fmaxf(fabsf(a[0][0]), fmaxf(fabsf(a[1][1]), fabsf(a[2][2])));
+	if (!(lmax >= 1e-6f)) return false;
+	float c3[3] = {0.f, 0.f, 0.f};
+	#pragma unroll
+	for (int k = 0; k < 3; k++) {
+		const float l = fabsf(a[k][k]);
+		if (fabsf(l - 1e-2f * lmax) <= 1e-4f * lmax) return false;
+		if (l < 1e-2f * lmax) continue;
+		const float proj = (v[0][k] * r[0] + v[1][k] * r[1] + v[2][k] * r[2]) / a[k][k];
+		#pragma unroll
+		for (int i = 0; i < 3; i++) c3[i] += v[i][k] * proj;
+	}
+	#pragma unroll
+	for (int i = 0; i < 3; i++) out[i] = fminf(fmaxf(m[i] + c3[i], 0.f), 1.f);
+	return true;
+}
+
+// QEF vertex and normal of one active cell whose origin is grid point p.
+// Pass 1 gathers the Hermite points of the cell's sign edges (cell-local:
+// 0/1 on the two other axes, t along the edge axis) and their mass point;
+// pass 2 accumulates the normal matrix and residual about the mass point in
+// FP32 (no cancellation: the points are centred first). Cells whose
+// truncation decision is within FP32 rounding take the FP64 solver.
+template<class E>
+__device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
+	const uint32_t *__restrict__ edge_map, const double *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
+	const uint32_t nx = g.n[0], ny = g.n[1];
+	const uint32_t sxy = nx * ny;
+	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
+	float P[12][3];
+	uint32_t eid[12];
+	uint32_t present = 0;
+	float ms[3] = {0.f, 0.f, 0.f};
+	int ne = 0;
+	#pragma unroll
+	for (int sl = 0; sl < 12; sl++) {
+		const int a = sl >> 2;
+		const uint32_t u = sl & 1, w = (sl >> 1) & 1;
+		const uint32_t stride = a == 0 ? 1u : (a == 1 ? nx : sxy);
+		const uint32_t ii = i + (a == 0 ? 0u : u), jj = j + (a == 0 ? u : (a == 1 ? 0u : w)), kk = k + (a == 2 ? 0u : w);
+		const uint32_t pe = (kk * ny + jj) * nx + ii;
+		eid[sl] = 0;
+		P[sl][0] = P[sl][1] = P[sl][2] = 0.f;
+		if ((__ldg(d + pe) < 0.f) == (__ldg(d + pe + stride) < 0.f)) continue;
+		eid[sl] = __ldg(edge_map + 3 * (uint64_t)pe + a);
+		const float t = (float)__ldg(edge_t + eid[sl]);
+		P[sl][0] = a == 0 ? t : (float)u;
+		P[sl][1] = a == 0 ? (float)u : (a == 1 ? t : (float)w);
+		P[sl][2] = a == 2 ? t : (float)w;
+		present |= 1u << sl;
+		ne++;
+		ms[0] += P[sl][0]; ms[1] += P[sl][1]; ms[2] += P[sl][2];
+	}
+	const float ine = ne > 0 ? 1.f / (float)ne : 0.f;
+	const float m[3] = {ne > 0 ? ms[0] * ine : 0.5f, ne > 0 ? ms[1] * ine : 0.5f, ne > 0 ? ms[2] * ine : 0.5f};
+	float A[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}}, rv[3] = {0.f, 0.f, 0.f};
+	#pragma unroll
+	for (int sl = 0; sl < 12; sl++) {
+		if (!(present >> sl & 1u)) continue;
+		const float *en = edge_n + 3 * (uint64_t)eid[sl];
+		const float nl[3] = {__ldg(en) * g.step[0], __ldg(en + 1) * g.step[1], __ldg(en + 2) * g.step[2]};
+		const float nn = sqrtf(nl[0] * nl[0] + nl[1] * nl[1] + nl[2] * nl[2]);
+		const float inn = nn > 0.f ? 1.f / nn : 0.f;
+		const float n[3] = {nl[0] * inn, nl[1] * inn, nl[2] * inn};
+		const float b = n[0] * (P[sl][0] - m[0]) + n[1] * (P[sl][1] - m[1]) + n[2] * (P[sl][2] - m[2]);
+		#pragma unroll
+		for (int x = 0; x < 3; x++) {
+			#pragma unroll
+			for (int y = 0; y < 3; y++) A[x][y] += n[x] * n[y];
+			rv[x] += n[x] * b;
+		}
+	}
+	float vc[3];
+	if (!dc_qef_solve_f32(A, rv, m, vc)) {
+		double vd[3];
+		dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
+		vc[0] = (float)vd[0]; vc[1] = (float)vd[1]; vc[2] = (float)vd[2];
+	}
+	const V3f vp = v3(dc_coord(g, 0, i) + vc[0] * g.step[0], dc_coord(g, 1, j) + vc[1] * g.step[1], dc_coord(g, 2, k) + vc[2] * g.step[2]);
 	vpos[0] = vp.x;
 	vpos[1] = vp.y;
 	vpos[2] = vp.z;

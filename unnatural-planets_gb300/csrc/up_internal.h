@@ -31,7 +31,7 @@ cudaError_t launch_synth_bwd(const up_synth_program &P, const float *xyz, uint64
 
 // ---- dual contouring (up_contour.cu)
 struct DcScratch {
-	uint32_t *blk_counts;   // 3 * nblocks
+	uint32_t *blk_counts;   // dc_scan_words(nblocks)
 	uint32_t *totals;       // 4 (device)
 	uint32_t *cell_map;     // cells
 	uint32_t *edge_map;     // 3 * points
@@ -42,6 +42,10 @@ struct DcScratch {
 	float *edge_n;          // 3 * capacity edges
 };
 uint32_t dc_num_blocks(const GridDev &g);
+// words of the block-count buffer for nb blocks (3 arrays + chunk sums)
+size_t dc_scan_words(uint32_t nb);
+// exclusive scan of the three block-count arrays in place; totals[a] = sums
+cudaError_t dc_scan_blocks(uint32_t *blk, uint32_t nb, uint32_t *totals, cudaStream_t s);
 // pass 1: counts -> totals[0]=cells, [1]=edges, [2]=quads (device), returns after enqueue
 cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s);
 // pass 2 (after the host knows the totals and sized the lists)
