@@ -12,6 +12,20 @@ end through the C ABI with pinned host output buffers.
 --impl reference times the reference algorithm's CPU path (the oracle's FP32
 restatement, per-sample callback, gradient by 6-tap central differences) on
 the host cores; under torchrun only rank 0 runs it.
+
+After the headline, rank 0 measures the other workloads of the path once
+each ("extras" in the JSON line, each bounded to seconds):
+  atlas      4096^2 texel atlas of the 512^3 planet's mesh (raster, synthetic
+             coloring program, dilation 7, 8-bit) into device buffers
+  adjoint    sphere - 4-octave simplex FBM: value+gradient forward and the
+             parameter adjoint of L = mean(d^2) on 16,777,216 shell points
+  batch      64 planets x 512 uneven chunks (1.8e8 samples): one batched
+             call (graph replay) against one up_contour call per chunk
+  fit        inverse fit, 300 Adam steps (lr 1e-2) on 32M shell points plus
+             a sign loss on the 256^3 grid
+  modes      reference-mode planet sphere/lakes/default, seed 0, 500^3 over
+             [-2000, 2000]^3, land+water+navigation in one pass
+  cpu_1t     the CPU baseline on one thread
 """
 from __future__ import annotations
 
@@ -122,6 +136,182 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _events(stream, fn, k):
+    """mean CUDA-event duration (ms) of k calls of fn on stream"""
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    torch.cuda.synchronize()
+    for a, b in evs:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / k
+
+
+def _guard(fn):
+    try:
+        return fn()
+    except Exception as e:  # reported in the JSON line, never hidden
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def extra_atlas(up, W, planet, stream, pos0, nrm0, idx0):
+    """4096^2 atlas of the 512^3 planet's mesh into device buffers"""
+    import ctypes as C
+    import torch
+    wh = 4096
+    p2, n2, uv, i2 = W.quad_atlas(pos0, nrm0, idx0, wh, wh)
+    dev = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    P, N, U, I = dev(p2), dev(n2), dev(uv), dev(i2.astype("int32"))
+    alb = torch.empty((wh, wh, 3), dtype=torch.uint8, device="cuda")
+    spc = torch.empty((wh, wh, 2), dtype=torch.uint8, device="cuda")
+    hgt = torch.empty((wh, wh), dtype=torch.uint8, device="cuda")
+    m = up.abi.MeshIn(P.data_ptr(), N.data_ptr(), U.data_ptr(), I.data_ptr(), int(p2.shape[0]), int(i2.shape[0]))
+    o = up.abi.TextureOut(alb.data_ptr(), spc.data_ptr(), hgt.data_ptr(), None, None, None)
+
+    def step():
+        st = planet.lib.up_texture(planet.h, up.abi.PURPOSE_LAND, C.byref(m), wh, wh, 7, C.byref(o))
+        assert st == 0, st
+    step()
+    ms = _events(stream, step, 5)
+    return {"ms": ms, "mtexels_s": wh * wh / ms / 1e3, "triangles": int(i2.shape[0]) // 3,
+            "what": "4096^2: raster + synthetic coloring (3-oct value albedo, 2-oct simplex roughness, height) + dilation 7 + U8"}
+
+
+def extra_adjoint(up, W, stream):
+    import torch
+    P = W.sphere_fbm()
+    planet = up.Planet(program=P)
+    planet.set_stream(stream.cuda_stream)
+    n = 1 << 24
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    d = torch.randn((n, 3), device="cuda", generator=gen)
+    d /= d.norm(dim=1, keepdim=True)
+    r = torch.empty(n, device="cuda").uniform_(0.95 ** 3, 1.05 ** 3, generator=gen).pow(1.0 / 3.0)
+    x = (d * r[:, None]).contiguous()
+    v = torch.empty(n, device="cuda")
+    g = torch.empty((n, 3), device="cuda")
+    nt = W.theta_count(P)
+    dth = torch.empty(nt, device="cuda")
+    fwd = lambda: planet.sdf_points(x, d=v, grad=g, want_grad=True)  # noqa: E731
+    fwd()
+    w = (2.0 / n) * v  # dL/dd of L = mean(d^2)
+    bwd = lambda: planet.param_backward(x, w, dtheta=dth)  # noqa: E731
+    bwd()
+    f_ms, b_ms = _events(stream, fwd, 5), _events(stream, bwd, 5)
+    return {"points": n, "theta": nt, "forward_ms": f_ms, "backward_ms": b_ms, "backward_gpoints_s": n / b_ms / 1e6,
+            "what": "sphere R=1 - 4-oct simplex FBM; forward value+dd/dp, backward dL/dtheta of mean(d^2), 0.05 shell"}
+
+
+def extra_batch(up, W, stream):
+    import ctypes as C
+    import torch
+    planets, chunks = W.chunk_set()
+    ctx = up.Planet(program=planets[0])
+    ctx.set_stream(stream.cuda_stream)
+    res = up.batch_run(ctx, planets, chunks, device=True)
+    up.batch_replay(ctx, res)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        up.batch_replay(ctx, res)
+    torch.cuda.synchronize()
+    batch_ms = 1e3 * (time.perf_counter() - t0) / reps
+    # one up_contour call per chunk into device buffers sized from the batch
+    vo, io = res["vertex_offsets"], res["index_offsets"]
+    ctxs = {}
+    for p, _ in chunks:
+        if p not in ctxs:
+            ctxs[p] = up.Planet(program=planets[p])
+            ctxs[p].set_stream(stream.cuda_stream)
+    vmax = int(max(vo[c + 1] - vo[c] for c in range(len(chunks))))
+    imax = int(max(io[c + 1] - io[c] for c in range(len(chunks))))
+    pos = torch.empty((max(vmax, 1), 3), device="cuda")
+    idx = torch.empty(max(imax, 1), dtype=torch.int32, device="cuda")
+
+    def per_chunk():
+        for p, g in chunks:
+            m = up.abi.MeshOut(pos.data_ptr(), None, idx.data_ptr(), vmax, imax, 0, 0)
+            st = ctxs[p].lib.up_contour(ctxs[p].h, 0, C.byref(g), None, C.byref(m))
+            assert st in (0, up.abi.UP_ERR_EMPTY_MESH), st
+    per_chunk()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    per_chunk()
+    torch.cuda.synchronize()
+    chunk_ms = 1e3 * (time.perf_counter() - t0)
+    samples = sum(g.count for _, g in chunks)
+    return {"chunks": len(chunks), "planets": len(planets), "samples": samples, "batched_ms": batch_ms,
+            "per_chunk_ms": chunk_ms, "speedup": chunk_ms / batch_ms, "batched_gsamples_s": samples / batch_ms / 1e6,
+            "vertices": int(vo[-1]), "triangles": int(io[-1]) // 3,
+            "what": "wall time: one up_batch_run (graph replay) vs one up_contour per chunk, device outputs"}
+
+
+def extra_fit(up, W, stream, steps=300):
+    import numpy as np
+    import torch
+    AG = importlib.import_module("unnatural-planets_gb300.autograd")
+    target = W.sphere_fbm(seed=5)
+    t_star = torch.from_numpy(W.theta_of(target)).cuda()
+    gen = torch.Generator(device="cuda").manual_seed(21)
+    n = 32 << 20
+    d = torch.randn((n, 3), device="cuda", generator=gen)
+    d /= d.norm(dim=1, keepdim=True)
+    r = torch.empty(n, device="cuda").uniform_(0.9 ** 3, 1.1 ** 3, generator=gen).pow(1.0 / 3.0)
+    x = (d * r[:, None]).contiguous()
+    gg = W.grid(W.GRID_C1, n=(256, 256, 256))
+    lo = torch.tensor(list(gg.lo), device="cuda")
+    hi = torch.tensor(list(gg.hi), device="cuda")
+    ax = [torch.linspace(float(lo[a]), float(hi[a]), 256, device="cuda") for a in range(3)]
+    zz, yy, xx = torch.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    xg = torch.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], dim=1).contiguous()
+    pt = up.Planet(program=target)
+    pt.set_stream(stream.cuda_stream)
+    d_star = pt.sdf_points(x, d=torch.empty(n, device="cuda"))
+    s_star = torch.sign(pt.sdf_points(xg, d=torch.empty(xg.shape[0], device="cuda")))
+    rng = np.random.default_rng(6)
+    t0 = t_star.cpu().numpy() * (1 + 0.15 * rng.uniform(-1, 1, size=t_star.shape[0])).astype(np.float32)
+    theta = torch.tensor(t0, device="cuda", requires_grad=True)
+    planet = up.Planet(program=W.sphere_fbm(seed=5))
+    planet.set_stream(stream.cuda_stream)
+    opt = torch.optim.Adam([theta], lr=1e-2)
+    err0 = float((theta.detach() - t_star).norm() / t_star.norm())
+
+    def step():
+        opt.zero_grad()
+        loss = ((AG.sdf(theta, x, planet) - d_star) ** 2).mean() + torch.relu(-AG.sdf(theta, xg, planet) * s_star).mean()
+        loss.backward()
+        opt.step()
+        return loss
+    step()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(steps - 1):
+        loss = step()
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t) / (steps - 1)
+    return {"steps": steps, "ms_per_step": ms, "points": n, "sign_points": int(xg.shape[0]), "loss": float(loss.detach()),
+            "theta_rel_err_start": err0, "theta_rel_err_end": float((theta.detach() - t_star).norm() / t_star.norm()),
+            "what": "sphere - 4-oct simplex FBM, theta* seed 5, theta0 = theta* (1 + 0.15 U[-1,1]) seed 6; "
+                    "L = mean((d - d*)^2) on 32M shell points + mean(relu(-d sign(d*))) on 256^3"}
+
+
+def extra_modes(up, stream):
+    import torch
+    planet = up.Planet("sphere", "lakes", "default", seed=0)
+    planet.set_stream(stream.cuda_stream)
+    g = up.abi.Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), (500, 500, 500))
+    n = g.count
+    outs = [torch.empty(n, device="cuda") for _ in range(3)]
+    fn = lambda: planet.sdf_grid(g, 7, outs=outs)  # noqa: E731
+    fn()
+    ms = _events(stream, fn, 3)
+    return {"ms": ms, "gsamples_s": n / ms / 1e6, "fields": 3,
+            "what": "sphere/lakes/default seed 0, 500^3 over [-2000,2000]^3, land+water+navigation in one pass"}
+
+
 def run_reference(args) -> None:
     ws, rank = _dist()
     if rank != 0:
@@ -215,7 +405,7 @@ def run_ours(args) -> None:
     t_plain = sum(plain_ms) / len(plain_ms)
 
     # full planet: sampling + dual contouring into device buffers
-    pos0, _, idx0 = planet.contour(grid)
+    pos0, nrm0, idx0 = planet.contour(grid)
     V, I = len(pos0), len(idx0)
     pos = torch.empty((V, 3), device="cuda")
     nrm = torch.empty((V, 3), device="cuda")
@@ -263,6 +453,16 @@ def run_ours(args) -> None:
     slabs = min(max(2 * threads, 16), args.grid)
     cpu_grad, cpu_s = cpu_rate(P, grid, slabs, threads, grad=True)
     cpu_plain, _ = cpu_rate(P, grid, slabs, threads, grad=False)
+    extras = {}
+    if not args.no_extras:
+        extras["atlas"] = _guard(lambda: extra_atlas(up, W, planet, stream, pos0, nrm0, idx0))
+        extras["adjoint"] = _guard(lambda: extra_adjoint(up, W, stream))
+        extras["batch"] = _guard(lambda: extra_batch(up, W, stream))
+        extras["fit"] = _guard(lambda: extra_fit(up, W, stream))
+        extras["modes"] = _guard(lambda: extra_modes(up, stream))
+        extras["cpu_1t"] = _guard(lambda: {"value": cpu_rate(P, grid, 1, 1, grad=True)[0] / 1e9,
+                                           "plain_value": cpu_rate(P, grid, 1, 1, grad=False)[0] / 1e9, "unit": UNIT,
+                                           "sample": f"1 z-slab of {args.grid}x{args.grid}, one thread"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_fused, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -286,6 +486,7 @@ def run_ours(args) -> None:
                          "plain_value": cpu_plain / 1e9, "cpu": _cpu_model()},
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
+        "extras": extras,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
@@ -299,6 +500,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", type=int, default=512, help="grid edge (512 is the benchmark; smaller for profiling captures)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads (atlas, adjoint, batch, fit, modes)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -52,3 +52,22 @@ def test_batch_rejects_bad_chunks(cuda, up):
     with pytest.raises(up.UpError) as e:
         up.batch_run(ctx, planets, chunks)
     assert e.value.status == up.abi.UP_ERR_INVALID_ARGUMENT
+
+
+def test_batch_replay_writes_live_buffers(cuda, up):
+    """batch_replay reuses the output struct of batch_run: the offset arrays
+    and outputs it points at must still be alive (collected garbage in
+    between), and the replay reproduces the first run."""
+    import gc
+    W = workloads()
+    planets, chunks = W.chunk_set(n_planets=3, n_chunks=12, seed=4, edge_lo=12, edge_hi=32)
+    ctx = up.Planet(program=planets[0])
+    res = up.batch_run(ctx, planets, chunks, values=True)
+    first = {k: np.copy(res[k]) for k in ("positions", "indices", "values")}
+    gc.collect()
+    junk = [np.full(1024, 7, np.uint64) for _ in range(256)]  # reuse of freed memory would show up here
+    for _ in range(3):
+        up.batch_replay(ctx, res)
+    for k in first:
+        assert np.array_equal(res[k], first[k]), k
+    assert all((j == 7).all() for j in junk)

@@ -188,10 +188,14 @@ def batch_run(planet_or_lib, planets, chunks, values=False, device=False):
         val = np.empty(nval, np.float32) if values else None
     o = abi.BatchOut(_addr(pos), _addr(idx), V, I, vo.ctypes.data, io.ctypes.data, 0, 0, _addr(val), nval if values else 0)
     ctx._check(ctx.lib.up_batch_run(ctx.h, P, len(planets), Cs, len(chunks), C.byref(o)))
-    return dict(positions=pos, indices=idx, vertex_offsets=vo.copy(), index_offsets=io.copy(), values=val, _args=(P, Cs, o))
+    # `o` holds raw addresses of vo/io and of the outputs: they stay referenced
+    # from _args so that batch_replay writes into live memory
+    return dict(positions=pos, indices=idx, vertex_offsets=vo.copy(), index_offsets=io.copy(), values=val,
+                _args=(P, Cs, o, vo, io, pos, idx, val))
 
 
 def batch_replay(ctx, prepared):
-    """Run the same batch again (graph replay inside the library)."""
-    P, Cs, o = prepared["_args"]
+    """Run the same batch again (graph replay inside the library), into the
+    output buffers of `prepared`."""
+    P, Cs, o = prepared["_args"][:3]
     ctx._check(ctx.lib.up_batch_run(ctx.h, P, len(P), Cs, len(Cs), C.byref(o)))
