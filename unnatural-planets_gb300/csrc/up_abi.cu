@@ -423,7 +423,7 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 		S.cell_list = (uint32_t *)buf(ctx, B_DC_CLIST, (size_t)ncells * 4);
 		S.edge_list = (uint32_t *)buf(ctx, B_DC_ELIST, (size_t)nedges * 4);
 		S.quad_list = (uint32_t *)buf(ctx, B_DC_QLIST, (size_t)nquads * 4);
-		S.edge_t = (double *)buf(ctx, B_DC_ET, (size_t)nedges * 8);
+		S.edge_t = (float *)buf(ctx, B_DC_ET, (size_t)nedges * 4);
 		S.edge_n = (float *)buf(ctx, B_DC_EN, (size_t)nedges * 12);
 		check(dc_emit(d, g, S, ctx->stream), "contour emit");
 		float *pos = (float *)stage_out(ctx, B_MESH_POS, mesh->positions, (size_t)ncells * 12);

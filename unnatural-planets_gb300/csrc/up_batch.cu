@@ -169,7 +169,7 @@ struct BatchEvalF {
 
 __global__ void __launch_bounds__(256) batch_hermite_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ edge_list,
-	double *__restrict__ edge_t, float *__restrict__ edge_n) {
+	float *__restrict__ edge_t, float *__restrict__ edge_n) {
 	const uint32_t *eoff = off + (nchunks + 1);
 	const uint32_t nedges = eoff[nchunks];
 	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nedges; e += gridDim.x * blockDim.x) {
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) batch_hermite_kernel(const up_synth_progr
 
 __global__ void __launch_bounds__(128) batch_qef_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ cell_list,
-	const uint32_t *__restrict__ edge_map, const double *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos) {
+	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos) {
 	const uint32_t ncells = off[nchunks];
 	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ncells; q += gridDim.x * blockDim.x) {
 		const uint32_t c = find_chunk(off, nchunks, q);
@@ -279,10 +279,10 @@ static cudaError_t enqueue_back(BatchState &S, cudaStream_t s) {
 		return need < (uint32_t)b ? (need ? need : 1u) : (uint32_t)b;
 	};
 	batch_hermite_kernel<<<grid_of((const void *)batch_hermite_kernel, 256, S.nedges), 256, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks,
-		S.grid.as<float>(), S.elist.as<uint32_t>(), S.et.as<double>(), S.en.as<float>());
+		S.grid.as<float>(), S.elist.as<uint32_t>(), S.et.as<float>(), S.en.as<float>());
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
 	batch_qef_kernel<<<grid_of((const void *)batch_qef_kernel, 128, S.ncells), 128, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
-		S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<double>(), S.en.as<float>(), S.pos.as<float>());
+		S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<float>(), S.en.as<float>(), S.pos.as<float>());
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
 	batch_quads_kernel<<<grid_of((const void *)batch_quads_kernel, 256, S.nquads), 256, 0, s>>>(C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
 		S.qlist.as<uint32_t>(), S.elist.as<uint32_t>(), S.cmap.as<uint32_t>(), S.idx.as<uint32_t>());
@@ -393,7 +393,7 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = S->clist.ensure((size_t)S->ncells * 4)) != cudaSuccess) return e;
 		if ((e = S->elist.ensure((size_t)S->nedges * 4)) != cudaSuccess) return e;
 		if ((e = S->qlist.ensure((size_t)S->nquads * 4)) != cudaSuccess) return e;
-		if ((e = S->et.ensure((size_t)S->nedges * 8)) != cudaSuccess) return e;
+		if ((e = S->et.ensure((size_t)S->nedges * 4)) != cudaSuccess) return e;
 		if ((e = S->en.ensure((size_t)S->nedges * 12)) != cudaSuccess) return e;
 		if ((e = S->pos.ensure((size_t)S->ncells * 12)) != cudaSuccess) return e;
 		if ((e = S->idx.ensure((size_t)S->nquads * 24)) != cudaSuccess) return e;

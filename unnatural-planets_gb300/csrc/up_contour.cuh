@@ -4,7 +4,8 @@
 // Rules (the CPU oracle implements the same rules independently):
 //   inside(d) = d < 0; a cell is active when its 8 corner signs differ; a
 //   sign edge joins two samples of different sign; the Hermite point is
-//   x0 + t (x1 - x0), t = d0 / (d0 - d1) in FP64; the Hermite normal is the
+//   x0 + t (x1 - x0), t = d0 / (d0 - d1) (FP32; the oracle uses FP64, a
+//   difference of ~1e-7 of a cell); the Hermite normal is the
 //   analytic gradient at that point; the cell vertex minimises the QEF
 //   (cell-local units, mass-point centred, eight cyclic Jacobi sweeps,
 //   eigenvalues below 1e-2 of the largest truncated, clamped to the cell)
@@ -151,21 +152,22 @@ __device__ inline void dc_qef_solve(int ne, const double (*pt)[3], const double 
 	for (int i = 0; i < 3; i++) out[i] = fmin(fmax(m[i] + c3[i], 0.0), 1.0);
 }
 
-// Hermite data of one sign edge (code = 3 * point + axis)
+// Hermite data of one sign edge (code = 3 * point + axis): the crossing
+// parameter t = d0 / (d0 - d1) and the unit analytic normal at the crossing
 template<class E>
-__device__ __forceinline__ void dc_hermite_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t code, double &t_out,
+__device__ __forceinline__ void dc_hermite_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t code, float &t_out,
 	float *n_out) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t p = code / 3, a = code % 3;
 	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
 	const uint32_t stride = a == 0 ? 1u : (a == 1 ? nx : nx * ny);
-	const double d0 = d[p], d1 = d[p + stride];
-	const double t = d0 / (d0 - d1);
-	double x[3] = {dc_coord(g, 0, i), dc_coord(g, 1, j), dc_coord(g, 2, k)};
+	const float d0 = d[p], d1 = d[p + stride];
+	const float t = d0 / (d0 - d1);
+	float x[3] = {dc_coord(g, 0, i), dc_coord(g, 1, j), dc_coord(g, 2, k)};
 	const uint32_t ii[3] = {i, j, k};
-	const double x1 = dc_coord(g, a, ii[a] + 1);
+	const float x1 = dc_coord(g, a, ii[a] + 1);
 	x[a] = x[a] + t * (x1 - x[a]);
-	const NG s = ev(v3((float)x[0], (float)x[1], (float)x[2]));
+	const NG s = ev(v3(x[0], x[1], x[2]));
 	const float ln = sqrtf(dot(s.g, s.g));
 	const float il = ln > 0.f ? 1.f / ln : 0.f;
 	t_out = t;
@@ -176,7 +178,7 @@ __device__ __forceinline__ void dc_hermite_item(const E &ev, const float *__rest
 
 // FP64 QEF vertex (cell-local) of one active cell whose origin is grid point p
 static __device__ __noinline__ void dc_qef_vertex_fp64(const float *__restrict__ d, const GridDev &g, uint32_t p, const uint32_t *__restrict__ edge_map,
-	const double *__restrict__ edge_t, const float *__restrict__ edge_n, double v[3]) {
+	const float *__restrict__ edge_t, const float *__restrict__ edge_n, double v[3]) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t sxy = nx * ny;
 	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
@@ -197,7 +199,7 @@ static __device__ __noinline__ void dc_qef_vertex_fp64(const float *__restrict__
 			const uint32_t pe = (kk * ny + jj) * nx + ii;
 			if ((d[pe] < 0.f) == (d[pe + stride] < 0.f)) continue;
 			const uint32_t eid = edge_map[3 * (uint64_t)pe + a];
-			const double t = edge_t[eid];
+			const double t = (double)edge_t[eid];
 			double h[3] = {dc_coord(g, 0, ii), dc_coord(g, 1, jj), dc_coord(g, 2, kk)};
 			const uint32_t iv[3] = {ii, jj, kk};
 			const double x1 = dc_coord(g, a, iv[a] + 1);
@@ -221,9 +223,11 @@ static __device__ __noinline__ void dc_qef_vertex_fp64(const float *__restrict__
 // FP32 form of dc_qef_solve for the accumulated A = sum n n^T and
 // r = sum n (n . (p - m)) about the mass point m: the same eight cyclic
 // Jacobi sweeps and truncation rule. Returns false when an eigenvalue lies
-// within 1e-4 lmax of the truncation threshold 1e-2 lmax, or lmax is below
-// 1e-6 (FP32 rounding of the eigenvalues is ~1e-7 lmax, so every other
-// truncation decision equals the FP64 one); the caller then solves in FP64.
+// within 2e-6 lmax of the truncation threshold 1e-2 lmax, or lmax is below
+// 1e-6 (the FP32 eigenvalues of this backward-stable iteration on a
+// matrix accumulated in FP32 are within a few 1e-7 lmax of the FP64 ones,
+// so every other truncation decision equals the FP64 one); the caller then
+// solves in FP64.
 __device__ __forceinline__ bool dc_qef_solve_f32(float a[3][3], const float r[3], const float m[3], float out[3]) {
 	float v[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
 	#pragma unroll 1
@@ -262,7 +266,7 @@ __device__ __forceinline__ bool dc_qef_solve_f32(float a[3][3], const float r[3]
 	#pragma unroll
 	for (int k = 0; k < 3; k++) {
 		const float l = fabsf(a[k][k]);
-		if (fabsf(l - 1e-2f * lmax) <= 1e-4f * lmax) return false;
+		if (fabsf(l - 1e-2f * lmax) <= 2e-6f * lmax) return false;
 		if (l < 1e-2f * lmax) continue;
 		const float proj = (v[0][k] * r[0] + v[1][k] * r[1] + v[2][k] * r[2]) / a[k][k];
 		#pragma unroll
@@ -281,7 +285,7 @@ __device__ __forceinline__ bool dc_qef_solve_f32(float a[3][3], const float r[3]
 // truncation decision is within FP32 rounding take the FP64 solver.
 template<class E>
 __device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
-	const uint32_t *__restrict__ edge_map, const double *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
+	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t sxy = nx * ny;
 	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
@@ -301,7 +305,7 @@ __device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict
 		P[sl][0] = P[sl][1] = P[sl][2] = 0.f;
 		if ((__ldg(d + pe) < 0.f) == (__ldg(d + pe + stride) < 0.f)) continue;
 		eid[sl] = __ldg(edge_map + 3 * (uint64_t)pe + a);
-		const float t = (float)__ldg(edge_t + eid[sl]);
+		const float t = __ldg(edge_t + eid[sl]);
 		P[sl][0] = a == 0 ? t : (float)u;
 		P[sl][1] = a == 0 ? (float)u : (a == 1 ? t : (float)w);
 		P[sl][2] = a == 2 ? t : (float)w;
@@ -367,7 +371,7 @@ __device__ __forceinline__ void dc_quad_item(const float *__restrict__ d, const 
 // Hermite data of every sign edge
 template<class E>
 __global__ void __launch_bounds__(256) dc_hermite_kernel(const E ev, const float *__restrict__ d, const GridDev g,
-	const uint32_t *__restrict__ edge_list, uint32_t nedges, double *__restrict__ edge_t, float *__restrict__ edge_n) {
+	const uint32_t *__restrict__ edge_list, uint32_t nedges, float *__restrict__ edge_t, float *__restrict__ edge_n) {
 	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nedges; e += gridDim.x * blockDim.x)
 		dc_hermite_item(ev, d, g, edge_list[e], edge_t[e], edge_n + 3 * (uint64_t)e);
 }
@@ -376,7 +380,7 @@ __global__ void __launch_bounds__(256) dc_hermite_kernel(const E ev, const float
 template<class E>
 __global__ void __launch_bounds__(128) dc_qef_kernel(const E ev, const float *__restrict__ d, const GridDev g,
 	const uint32_t *__restrict__ cell_list, uint32_t ncells, const uint32_t *__restrict__ edge_map,
-	const double *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm) {
+	const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm) {
 	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x)
 		dc_qef_item(ev, d, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nrm ? nrm + 3 * (uint64_t)c : nullptr);
 }

@@ -38,7 +38,7 @@ struct DcScratch {
 	uint32_t *cell_list;    // capacity cells
 	uint32_t *edge_list;    // capacity edges
 	uint32_t *quad_list;    // capacity quads
-	double *edge_t;         // capacity edges
+	float *edge_t;         // capacity edges
 	float *edge_n;          // 3 * capacity edges
 };
 uint32_t dc_num_blocks(const GridDev &g);
