@@ -35,7 +35,7 @@ using namespace up;
 
 enum BufSlot {
 	B_IN0, B_OUT0, B_OUT1, B_OUT2, B_GRAD, B_GRID, B_PARTIALS, B_W,
-	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN,
+	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS,
 	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
 	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
@@ -410,6 +410,7 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 		S.totals = (uint32_t *)buf(ctx, B_DC_TOT, 16);
 		S.cell_map = (uint32_t *)buf(ctx, B_DC_CMAP, nc * 4);
 		S.edge_map = (uint32_t *)buf(ctx, B_DC_EMAP, np * 12);
+		S.signs = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(g) * 4);
 		check(dc_count(d, g, S, ctx->stream), "contour count");
 		uint32_t tot[4] = {0, 0, 0, 0};
 		check(cudaMemcpyAsync(tot, S.totals, 12, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync totals");

@@ -12,9 +12,11 @@
 //   in FP32, and in FP64 for the cells whose truncation decision lies
 //   within FP32 rounding;
 //   every sign edge with four cells emits two triangles wound outwards.
-// Pipeline: count (per 1024-point block: active cells, sign edges, quads) ->
+// Pipeline (single grids): signs (d < 0 bit-packed, 32 points a word) ->
+// count (per word: active cells, sign edges, quads; dc_word_flags) ->
 // exclusive scan of block counts -> emit (ordered lists and dense maps; order
 // fixed by the scan, no atomics) -> Hermite per edge -> QEF per cell -> quads.
+// Batches of chunks classify per point (point_flags, up_batch.cu).
 #pragma once
 #include "up_internal.h"
 #include "up_noise.cuh"
@@ -53,6 +55,69 @@ __device__ __forceinline__ PointFlags point_flags(const float *__restrict__ d, c
 	}
 	return f;
 }
+// ---- word-parallel classification (single grids)
+// The signs (d < 0) of 32 consecutive points form one word (bit b = point
+// 32 w + b; 0 past the grid; two words of zero padding). One thread
+// classifies a word: the neighbour signs along +x, +y, +z are the same
+// bitfield read at offsets 1, nx, nx * ny (funnel shifts of two words), so
+// sign-change edges, quads and active cells are bitwise expressions, gated
+// by per-word masks of the grid boundary conditions of point_flags.
+constexpr uint32_t DC_WPB = DC_T * 32; // points per block of the word kernels
+
+__device__ __forceinline__ uint32_t dc_bits_at(const uint32_t *__restrict__ B, uint64_t q, uint64_t nalloc) {
+	const uint64_t wi = q >> 5;
+	const uint32_t lo = wi < nalloc ? __ldg(B + wi) : 0u, hi = wi + 1 < nalloc ? __ldg(B + wi + 1) : 0u;
+	return __funnelshift_r(lo, hi, (uint32_t)(q & 31));
+}
+struct WordFlags { uint32_t cell, ex, ey, ez, qx, qy, qz; };
+__device__ __forceinline__ WordFlags dc_word_flags(const uint32_t *__restrict__ B, uint64_t nalloc, const GridDev &g, uint64_t w, uint32_t npts) {
+	WordFlags f{0, 0, 0, 0, 0, 0, 0};
+	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const uint64_t p0 = 32 * w;
+	if (p0 >= npts) return f;
+	// boundary masks: bits of points with i + 1 < nx (hx), 1 <= i < nx - 1 (iix),
+	// j + 1 < ny (hy), 1 <= j < ny - 1 (ijy) and likewise in k
+	uint32_t valid = 0, hx = 0, iix = 0, hy = 0, ijy = 0, hz = 0, ikz = 0;
+	uint32_t r = (uint32_t)(p0 / nx), i = (uint32_t)(p0 - (uint64_t)r * nx), pos = 0;
+	while (pos < 32 && p0 + pos < npts) {
+		uint32_t seg = 32 - pos;
+		if (nx - i < seg) seg = nx - i;
+		if (npts - (p0 + pos) < seg) seg = (uint32_t)(npts - (p0 + pos));
+		const uint32_t sm = (seg >= 32 ? 0xFFFFFFFFu : ((1u << seg) - 1u)) << pos;
+		const uint32_t j = r % ny, k = r / ny;
+		valid |= sm;
+		if (j + 1 < ny) hy |= sm;
+		if (j >= 1 && j + 1 < ny) ijy |= sm;
+		if (k + 1 < nz) hz |= sm;
+		if (k >= 1 && k + 1 < nz) ikz |= sm;
+		uint32_t mx = sm, mi = sm;
+		if (i + seg == nx) { mx &= ~(1u << (pos + seg - 1)); mi &= ~(1u << (pos + seg - 1)); }
+		if (i == 0) mi &= ~(1u << pos);
+		hx |= mx;
+		iix |= mi;
+		pos += seg;
+		i = 0;
+		r++;
+	}
+	const uint64_t sxy = (uint64_t)nx * ny;
+	const uint32_t A = dc_bits_at(B, p0, nalloc), X = dc_bits_at(B, p0 + 1, nalloc);
+	const uint32_t Y = dc_bits_at(B, p0 + nx, nalloc), XY = dc_bits_at(B, p0 + nx + 1, nalloc);
+	const uint32_t Z = dc_bits_at(B, p0 + sxy, nalloc), ZX = dc_bits_at(B, p0 + sxy + 1, nalloc);
+	const uint32_t ZY = dc_bits_at(B, p0 + sxy + nx, nalloc), ZXY = dc_bits_at(B, p0 + sxy + nx + 1, nalloc);
+	f.ex = (A ^ X) & hx;
+	f.ey = (A ^ Y) & hy;
+	f.ez = (A ^ Z) & hz;
+	f.qx = f.ex & ijy & ikz;
+	f.qy = f.ey & iix & ikz;
+	f.qz = f.ez & iix & ijy;
+	f.cell = ((A ^ X) | (A ^ Y) | (A ^ XY) | (A ^ Z) | (A ^ ZX) | (A ^ ZY) | (A ^ ZXY)) & hx & hy & hz;
+	return f;
+}
+__device__ __forceinline__ uint64_t dc_word_counts(const WordFlags &f) {
+	return (uint64_t)__popc(f.cell) | ((uint64_t)(__popc(f.ex) + __popc(f.ey) + __popc(f.ez)) << 21) |
+		((uint64_t)(__popc(f.qx) + __popc(f.qy) + __popc(f.qz)) << 42);
+}
+
 __device__ __forceinline__ uint64_t pack_counts(PointFlags f) {
 	const uint64_t c = f.bits & 1u;
 	const uint64_t e = __popc(f.bits & 14u);

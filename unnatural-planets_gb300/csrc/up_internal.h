@@ -40,8 +40,10 @@ struct DcScratch {
 	uint32_t *quad_list;    // capacity quads
 	float *edge_t;         // capacity edges
 	float *edge_n;          // 3 * capacity edges
+	uint32_t *signs;        // dc_sign_words(grid): bit-packed d < 0
 };
 uint32_t dc_num_blocks(const GridDev &g);
+uint64_t dc_sign_words(const GridDev &g);
 // words of the block-count buffer for nb blocks (3 arrays + chunk sums)
 size_t dc_scan_words(uint32_t nb);
 // exclusive scan of the three block-count arrays in place; totals[a] = sums
