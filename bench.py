@@ -46,6 +46,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "SDF+grad Gsamples/s at 512^3 (fused value+gradient; plain and ms/planet alongside)"
 UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
+# DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
+# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (243.29 MB / 16,777,216)
+TRAFFIC_PER_SAMPLE_FUSED = 243.290368e6 / 16777216
 
 
 def _pkg():
@@ -477,10 +480,16 @@ def run_ours(args) -> None:
         "e2e": {"value": ws * N / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 * N,
                 "what": "up_sdf_grid value+gradient into pinned host buffers"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                     "traffic": None,
+                     "traffic": TRAFFIC_PER_SAMPLE_FUSED * N,
+                     "traffic_source": "dram read+write of synth_grid_runs_kernel<1,2,1301> from one ncu capture at 256^3 "
+                                       f"({TRAFFIC_PER_SAMPLE_FUSED:.2f} B/sample), scaled by samples to this launch",
                      "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x {max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)",
                      "flops_per_sample": W.FLOPS_PER_SAMPLE_C2,
-                     "note": "value-path FLOPs of the oracle count; the gradient's extra arithmetic and all integer hashing are not counted"},
+                     "note": "value-path FLOPs of the oracle count; the gradient's extra arithmetic and all integer hashing are not counted; "
+                             "the kernel is issue-bound on the ALU pipe (hashing), see profiles/",
+                     "hbm_view": {"algorithmic_bytes": 16 * N, "achieved_gbs": 16 * N / (t_fused * 1e-3) / 1e9,
+                                  "peak_gbs": peaks.get("hbm_gbs"), "frac": (16 * N / (t_fused * 1e-3) / 1e9) / peaks["hbm_gbs"]
+                                  if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}},
         "cpu_baseline": {"value": cpu_grad / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{slabs} z-slabs of {args.grid}x{args.grid} per leg; value+gradient by 6-tap central differences",
                          "plain_value": cpu_plain / 1e9, "cpu": _cpu_model()},
