@@ -232,6 +232,34 @@ int up_sdf_grid(up_context *ctx, uint32_t fields_mask, const up_grid *grid, floa
  * vertex_count/index_count filled in. UP_ERR_EMPTY_MESH if no triangles. */
 int up_contour(up_context *ctx, int field, const up_grid *grid, const float *values, up_mesh_out *mesh);
 
+/* Base mesh of one field, as meshGenerateBaseLand / Water / Navigation
+ * (meshGeneration.cpp:46-108): the up_contour mesh, then
+ *  - only the largest connected component kept (meshRemoveDisconnected,
+ *    :41): components of the vertex graph joined by triangles, largest =
+ *    most triangles, ties to the component holding the lowest vertex index;
+ *  - meshFlipNormals (:42) needs nothing: up_contour already emits that
+ *    orientation;
+ *  - WATER only (:62-95): a vertex is valid when the raw elevation there is
+ *    below 0.1; validity spreads twice to all vertices of every triangle
+ *    holding a valid vertex; triangles with an invalid vertex and invalid
+ *    vertices are removed (meshRemoveInvalid).
+ * Kept vertices and triangles keep their order. Same capacity protocol and
+ * errors as up_contour (UP_ERR_EMPTY_MESH when nothing is left). */
+int up_mesh_generate_base(up_context *ctx, int field, const up_grid *grid, const float *values, up_mesh_out *mesh);
+
+/* ---------------------------------------------------------------- images */
+/* imageConvertSpecialToGltfPbr (generator.cpp:135): special (width*height*2
+ * u8: roughness, metallic) -> pbr (width*height*3 u8) = (255, roughness,
+ * metallic), the glTF metallicRoughness channel convention. Host or device
+ * buffers. */
+int up_image_special_to_gltf_pbr(up_context *ctx, const uint8_t *special, uint32_t width, uint32_t height, uint8_t *pbr);
+/* imageConvertHeigthToNormal(height, strength) (generator.cpp:137): height
+ * map (width*height u8) -> tangent-space normal map (width*height*3 u8):
+ * h = height/255, n = normalize(-strength dh/dx, -strength dh/dy, 1) with
+ * central differences in texels (one-sided at the border, x along a row, y
+ * down the rows), stored as (n + 1)/2 * 255 rounded. Host or device buffers. */
+int up_image_height_to_normal(up_context *ctx, const uint8_t *height_map, uint32_t width, uint32_t height, float strength, uint8_t *normal);
+
 /* ---------------------------------------------------------------- texels */
 /* Per-texel material of an unwrapped mesh: replaces Generator<Water>::generate
  * (textures.cpp:45-82): UV rasterisation (meshGenerateTexture, :66-71), the

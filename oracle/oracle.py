@@ -62,6 +62,7 @@ def lib(fast: bool = False) -> C.CDLL:
         "orc_tiles": (None, [vp, C.c_int, vp, vp, C.c_uint64, vp, vp, C.c_int]),
         "orc_texture": (None, [vp, C.POINTER(abi.SynthProgram), C.c_int, vp, vp, vp, vp, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int,
                                vp, vp, vp, vp, vp, vp, vp, C.c_int]),
+        "orc_mesh_filter": (None, [C.c_uint32, C.c_uint32, vp, vp, vp, vp]),
     }
     for n, (res, args) in sigs.items():
         f = getattr(L, n)
@@ -214,3 +215,48 @@ def texture(purpose, pos, nrm, uv, idx, W, H, dilation=7, planet=None, program=N
                       _p(nrm), _p(uv), _p(idx), idx.shape[0], W, H, dilation, _p(r["albedo_f"]), _p(r["special_f"]),
                       _p(r["height_f"]), _p(r["albedo"]), _p(r["special"]), _p(r["height"]), _p(r["owner"]), threads)
     return r
+
+
+def mesh_filter(pos, nrm, idx, valid=None):
+    """meshGenerateBase* hygiene on a contoured mesh (orc_mesh_filter):
+    largest component, and for water (valid = per-vertex elevationRaw < 0.1)
+    the two-ring filter; then ordered compaction. Returns (pos, nrm, idx)."""
+    idx = np.ascontiguousarray(idx, np.uint32)
+    V, T = int(pos.shape[0]), int(idx.shape[0]) // 3
+    keep_v = np.zeros(V, np.uint8)
+    keep_t = np.zeros(T, np.uint8)
+    va = None if valid is None else np.ascontiguousarray(valid, np.uint8)
+    lib().orc_mesh_filter(V, T, _p(idx), _p(va), _p(keep_v), _p(keep_t))
+    kv, kt = keep_v.astype(bool), keep_t.astype(bool)
+    newidx = np.cumsum(kv) - 1
+    tri = idx.reshape(-1, 3)[kt]
+    return pos[kv], (None if nrm is None else nrm[kv]), newidx[tri].reshape(-1).astype(np.uint32)
+
+
+def special_to_gltf_pbr(special: np.ndarray) -> np.ndarray:
+    """imageConvertSpecialToGltfPbr, project definition: (255, roughness, metallic)."""
+    h, w = special.shape[:2]
+    out = np.empty((h, w, 3), np.uint8)
+    out[..., 0] = 255
+    out[..., 1:] = special
+    return out
+
+
+def height_to_normal(height: np.ndarray, strength: float = 1.0) -> np.ndarray:
+    """imageConvertHeigthToNormal, project definition: h = height/255,
+    n = normalize(-s dh/dx, -s dh/dy, 1), central differences in texels,
+    one-sided at the border; (n + 1)/2 * 255 rounded. FP64."""
+    h = height.astype(np.float64)
+    dx = np.zeros_like(h)
+    dy = np.zeros_like(h)
+    if h.shape[1] > 1:
+        dx[:, 1:-1] = 0.5 * (h[:, 2:] - h[:, :-2])
+        dx[:, 0] = h[:, 1] - h[:, 0]
+        dx[:, -1] = h[:, -1] - h[:, -2]
+    if h.shape[0] > 1:
+        dy[1:-1, :] = 0.5 * (h[2:, :] - h[:-2, :])
+        dy[0, :] = h[1, :] - h[0, :]
+        dy[-1, :] = h[-1, :] - h[-2, :]
+    n = np.stack([-strength * dx / 255.0, -strength * dy / 255.0, np.ones_like(h)], axis=-1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    return np.floor(np.clip(n * 0.5 + 0.5, 0, 1) * 255 + 0.5).astype(np.uint8)

@@ -373,4 +373,64 @@ void orc_texture(void *planet, const up_synth_program *prog, int purpose, const 
 	if (owner) std::copy(R.owner.begin(), R.owner.end(), owner);
 }
 
+// Mesh hygiene of meshGenerateBase* (meshGeneration.cpp:41, 62-95), the
+// project definitions restated sequentially: union-find over the vertex graph
+// joined by triangles; kept component = most triangles, ties to the one
+// holding the lowest vertex index; water (valid != NULL: the per-vertex test
+// elevationRaw < 0.1, already evaluated): validity restricted to the kept
+// component, two expansions over its triangles reading the previous pass,
+// then triangles with an invalid vertex dropped. Outputs 0/1 keep flags.
+void orc_mesh_filter(uint32_t V, uint32_t T, const uint32_t *idx, const uint8_t *valid, uint8_t *keep_v, uint8_t *keep_t) {
+	std::vector<uint32_t> parent(V);
+	for (uint32_t v = 0; v < V; v++) parent[v] = v;
+	auto find = [&](uint32_t x) {
+		while (parent[x] != x) {
+			parent[x] = parent[parent[x]];
+			x = parent[x];
+		}
+		return x;
+	};
+	auto unite = [&](uint32_t a, uint32_t b) {
+		a = find(a);
+		b = find(b);
+		if (a == b) return;
+		if (a < b) parent[b] = a;
+		else parent[a] = b;
+	};
+	for (uint32_t t = 0; t < T; t++) {
+		unite(idx[3 * t], idx[3 * t + 1]);
+		unite(idx[3 * t], idx[3 * t + 2]);
+	}
+	std::vector<uint64_t> tri(V, 0);
+	for (uint32_t t = 0; t < T; t++) tri[find(idx[3 * t])]++;
+	uint32_t root = 0;
+	uint64_t most = 0;
+	bool any = false;
+	for (uint32_t v = 0; v < V; v++) // roots are the lowest vertex of their component; ascending order breaks ties
+		if (find(v) == v && (!any || tri[v] > most)) {
+			root = v;
+			most = tri[v];
+			any = true;
+		}
+	std::vector<uint8_t> in(V);
+	for (uint32_t v = 0; v < V; v++) in[v] = find(v) == root;
+	if (!valid) {
+		for (uint32_t v = 0; v < V; v++) keep_v[v] = in[v];
+		for (uint32_t t = 0; t < T; t++) keep_t[t] = in[idx[3 * t]];
+		return;
+	}
+	std::vector<uint8_t> ok(V), ok2;
+	for (uint32_t v = 0; v < V; v++) ok[v] = in[v] && valid[v];
+	for (int r = 0; r < 2; r++) {
+		ok2 = ok;
+		for (uint32_t t = 0; t < T; t++) {
+			const uint32_t a = idx[3 * t], b = idx[3 * t + 1], c = idx[3 * t + 2];
+			if (in[a] && (ok[a] || ok[b] || ok[c])) ok2[a] = ok2[b] = ok2[c] = 1;
+		}
+		ok.swap(ok2);
+	}
+	for (uint32_t v = 0; v < V; v++) keep_v[v] = ok[v];
+	for (uint32_t t = 0; t < T; t++) keep_t[t] = ok[idx[3 * t]] && ok[idx[3 * t + 1]] && ok[idx[3 * t + 2]];
+}
+
 } // extern "C"

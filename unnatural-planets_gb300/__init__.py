@@ -114,6 +114,35 @@ class Planet:
         self._check(self.lib.up_contour(self.h, field, C.byref(grid), _addr(values), C.byref(m)))
         return pos, nrm, idx
 
+    def mesh_generate_base(self, grid: abi.Grid, field=abi.FIELD_LAND, values=None, normals=True):
+        """up_mesh_generate_base: contour, largest component, water filter.
+        Returns (positions (V,3), normals (V,3) or None, indices (I,)) as numpy."""
+        m = abi.MeshOut()
+        st = self.lib.up_mesh_generate_base(self.h, field, C.byref(grid), _addr(values), C.byref(m))
+        if st != abi.UP_ERR_CAPACITY:
+            self._check(st)
+        V, I = int(m.vertex_count), int(m.index_count)
+        pos = np.empty((V, 3), np.float32)
+        nrm = np.empty((V, 3), np.float32) if normals else None
+        idx = np.empty(I, np.uint32)
+        m = abi.MeshOut(pos.ctypes.data, nrm.ctypes.data if normals else None, idx.ctypes.data, V, I, 0, 0)
+        self._check(self.lib.up_mesh_generate_base(self.h, field, C.byref(grid), _addr(values), C.byref(m)))
+        return pos, nrm, idx
+
+    def special_to_gltf_pbr(self, special):
+        """(H, W, 2) uint8 special image -> (H, W, 3) uint8 glTF metallicRoughness."""
+        h, w = int(special.shape[0]), int(special.shape[1])
+        out = np.empty((h, w, 3), np.uint8)
+        self._check(self.lib.up_image_special_to_gltf_pbr(self.h, _addr(special), w, h, _addr(out)))
+        return out
+
+    def height_to_normal(self, height, strength=1.0):
+        """(H, W) uint8 height map -> (H, W, 3) uint8 normal map."""
+        h, w = int(height.shape[0]), int(height.shape[1])
+        out = np.empty((h, w, 3), np.uint8)
+        self._check(self.lib.up_image_height_to_normal(self.h, _addr(height), w, h, float(strength), _addr(out)))
+        return out
+
     def param_backward(self, xyz, dL_dd, dtheta=None):
         n = int(xyz.shape[0])
         nt = int(self.lib.up_synth_theta_count(C.byref(self.program)))

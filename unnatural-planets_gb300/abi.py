@@ -118,6 +118,9 @@ SIGNATURES = [
     ("up_sdf_navigation", C.c_float, [C.c_void_p]),
     ("up_sdf_grid", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Grid), C.c_void_p * 3, C.c_void_p]),
     ("up_contour", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Grid), C.c_void_p, C.POINTER(MeshOut)]),
+    ("up_mesh_generate_base", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Grid), C.c_void_p, C.POINTER(MeshOut)]),
+    ("up_image_special_to_gltf_pbr", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("up_image_height_to_normal", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]),
     ("up_texture", C.c_int, [C.c_void_p, C.c_int, C.POINTER(MeshIn), C.c_uint32, C.c_uint32, C.c_int, C.POINTER(TextureOut)]),
     ("up_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(TileOut)]),
     ("up_sdf_param_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),

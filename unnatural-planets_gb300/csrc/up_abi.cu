@@ -39,6 +39,8 @@ enum BufSlot {
 	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
 	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
+	B_BASE_POS, B_BASE_NRM, B_BASE_IDX, B_BASE_ELEV, B_BASE_PARENT, B_BASE_LABEL, B_BASE_CNT, B_BASE_NEWIDX, B_BASE_BLK, B_BASE_SMALL,
+	B_BASE_KEEPV, B_BASE_VALID2, B_BASE_KEEPT,
 	B_COUNT
 };
 
@@ -182,6 +184,62 @@ bool valid_program(const up_synth_program &p) {
 		if (L.distance < 0 || L.distance > 2 || L.operation < 0 || L.operation > 6) return false;
 	}
 	return true;
+}
+
+// Contouring in two steps (shared by up_contour and up_mesh_generate_base):
+// sampling (or staging the caller's values) and counting, then, once the
+// caller has sized the outputs, emission and geometry into device pointers.
+struct ContourRun {
+	GridDev g;
+	const float *d = nullptr;
+	DcScratch S{};
+	uint32_t ncells = 0, nedges = 0, nquads = 0;
+};
+int contour_count(up_context *ctx, int field, const up_grid *grid, const float *values, ContourRun &c) {
+	c.g = make_grid(*grid);
+	const size_t np = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
+	const size_t nc = (size_t)(grid->n[0] - 1) * (grid->n[1] - 1) * (grid->n[2] - 1);
+	if (values) {
+		c.d = (const float *)stage_in(ctx, B_GRID, values, np * 4);
+	} else {
+		float *gd = (float *)buf(ctx, B_GRID, np * 4);
+		reset_flag(ctx);
+		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		else {
+			float *o[3] = {nullptr, nullptr, nullptr};
+			o[field] = gd;
+			check(launch_modes_grid(ctx->d_modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		}
+		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
+		c.d = gd;
+	}
+	DcScratch &S = c.S;
+	const uint32_t nb = dc_num_blocks(c.g);
+	S.blk_counts = (uint32_t *)buf(ctx, B_DC_BLK, dc_scan_words(nb) * 4);
+	S.totals = (uint32_t *)buf(ctx, B_DC_TOT, 16);
+	S.cell_map = (uint32_t *)buf(ctx, B_DC_CMAP, nc * 4);
+	S.edge_map = (uint32_t *)buf(ctx, B_DC_EMAP, np * 12);
+	S.signs = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(c.g) * 4);
+	check(dc_count(c.d, c.g, S, ctx->stream), "contour count");
+	uint32_t tot[4] = {0, 0, 0, 0};
+	check(cudaMemcpyAsync(tot, S.totals, 12, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync totals");
+	check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+	c.ncells = tot[0];
+	c.nedges = tot[1];
+	c.nquads = tot[2];
+	if (c.nquads == 0) return fail(ctx, UP_ERR_EMPTY_MESH, std::string("generated empty base ") + field_word(field) + " mesh");
+	return UP_OK;
+}
+void contour_geometry(up_context *ctx, int field, ContourRun &c, float *pos, float *nrm, uint32_t *idx) {
+	DcScratch &S = c.S;
+	S.cell_list = (uint32_t *)buf(ctx, B_DC_CLIST, (size_t)c.ncells * 4);
+	S.edge_list = (uint32_t *)buf(ctx, B_DC_ELIST, (size_t)c.nedges * 4);
+	S.quad_list = (uint32_t *)buf(ctx, B_DC_QLIST, (size_t)c.nquads * 4);
+	S.edge_t = (float *)buf(ctx, B_DC_ET, (size_t)c.nedges * 4);
+	S.edge_n = (float *)buf(ctx, B_DC_EN, (size_t)c.nedges * 12);
+	check(dc_emit(c.d, c.g, S, ctx->stream), "contour emit");
+	if (ctx->synthetic) check(dc_geometry_synth(ctx->prog, c.d, c.g, S, c.ncells, c.nedges, c.nquads, pos, nrm, idx, ctx->stream), "contour geometry");
+	else check(dc_geometry_modes(ctx->d_modes, field, c.d, c.g, S, c.ncells, c.nedges, c.nquads, pos, nrm, idx, ctx->stream), "contour geometry");
 }
 
 } // namespace
@@ -386,55 +444,110 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
 	return guarded(ctx, [&]() {
 		set_device(ctx);
-		const GridDev g = make_grid(*grid);
-		const size_t np = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
-		const size_t nc = (size_t)(grid->n[0] - 1) * (grid->n[1] - 1) * (grid->n[2] - 1);
-		const float *d;
-		if (values) {
-			d = (const float *)stage_in(ctx, B_GRID, values, np * 4);
-		} else {
-			float *gd = (float *)buf(ctx, B_GRID, np * 4);
-			reset_flag(ctx);
-			if (ctx->synthetic) check(launch_synth_grid(ctx->prog, g, gd, nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
-			else {
-				float *o[3] = {nullptr, nullptr, nullptr};
-				o[field] = gd;
-				check(launch_modes_grid(ctx->d_modes, 1u << field, g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
-			}
-			if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
-			d = gd;
-		}
-		DcScratch S;
-		const uint32_t nb = dc_num_blocks(g);
-		S.blk_counts = (uint32_t *)buf(ctx, B_DC_BLK, dc_scan_words(nb) * 4);
-		S.totals = (uint32_t *)buf(ctx, B_DC_TOT, 16);
-		S.cell_map = (uint32_t *)buf(ctx, B_DC_CMAP, nc * 4);
-		S.edge_map = (uint32_t *)buf(ctx, B_DC_EMAP, np * 12);
-		S.signs = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(g) * 4);
-		check(dc_count(d, g, S, ctx->stream), "contour count");
-		uint32_t tot[4] = {0, 0, 0, 0};
-		check(cudaMemcpyAsync(tot, S.totals, 12, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync totals");
-		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-		const uint32_t ncells = tot[0], nedges = tot[1], nquads = tot[2];
-		mesh->vertex_count = ncells;
-		mesh->index_count = 6ull * nquads;
-		if (nquads == 0) return fail(ctx, UP_ERR_EMPTY_MESH, std::string("generated empty base ") + field_word(field) + " mesh");
-		if (!mesh->positions || !mesh->indices || mesh->vertex_capacity < ncells || mesh->index_capacity < 6ull * nquads)
+		ContourRun c;
+		const int st = contour_count(ctx, field, grid, values, c);
+		if (st != UP_OK) return st;
+		mesh->vertex_count = c.ncells;
+		mesh->index_count = 6ull * c.nquads;
+		if (!mesh->positions || !mesh->indices || mesh->vertex_capacity < c.ncells || mesh->index_capacity < 6ull * c.nquads)
 			return fail(ctx, UP_ERR_CAPACITY, "mesh buffers too small");
-		S.cell_list = (uint32_t *)buf(ctx, B_DC_CLIST, (size_t)ncells * 4);
-		S.edge_list = (uint32_t *)buf(ctx, B_DC_ELIST, (size_t)nedges * 4);
-		S.quad_list = (uint32_t *)buf(ctx, B_DC_QLIST, (size_t)nquads * 4);
-		S.edge_t = (float *)buf(ctx, B_DC_ET, (size_t)nedges * 4);
-		S.edge_n = (float *)buf(ctx, B_DC_EN, (size_t)nedges * 12);
-		check(dc_emit(d, g, S, ctx->stream), "contour emit");
-		float *pos = (float *)stage_out(ctx, B_MESH_POS, mesh->positions, (size_t)ncells * 12);
-		float *nrm = (float *)stage_out(ctx, B_MESH_NRM, mesh->normals, (size_t)ncells * 12);
-		uint32_t *idx = (uint32_t *)stage_out(ctx, B_MESH_IDX, mesh->indices, (size_t)nquads * 24);
-		if (ctx->synthetic) check(dc_geometry_synth(ctx->prog, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
-		else check(dc_geometry_modes(ctx->d_modes, field, d, g, S, ncells, nedges, nquads, pos, nrm, idx, ctx->stream), "contour geometry");
-		finish_out(ctx, mesh->positions, pos, (size_t)ncells * 12);
-		finish_out(ctx, mesh->normals, nrm, (size_t)ncells * 12);
-		finish_out(ctx, mesh->indices, idx, (size_t)nquads * 24);
+		float *pos = (float *)stage_out(ctx, B_MESH_POS, mesh->positions, (size_t)c.ncells * 12);
+		float *nrm = (float *)stage_out(ctx, B_MESH_NRM, mesh->normals, (size_t)c.ncells * 12);
+		uint32_t *idx = (uint32_t *)stage_out(ctx, B_MESH_IDX, mesh->indices, (size_t)c.nquads * 24);
+		contour_geometry(ctx, field, c, pos, nrm, idx);
+		finish_out(ctx, mesh->positions, pos, (size_t)c.ncells * 12);
+		finish_out(ctx, mesh->normals, nrm, (size_t)c.ncells * 12);
+		finish_out(ctx, mesh->indices, idx, (size_t)c.nquads * 24);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_mesh_generate_base(up_context *ctx, int field, const up_grid *grid, const float *values, up_mesh_out *mesh) {
+	if (!ctx || !valid_grid(grid) || !mesh) return UP_ERR_INVALID_ARGUMENT;
+	if (field < 0 || field > 2) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "base mesh field must be LAND, WATER or NAVIGATION");
+	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		ContourRun c;
+		const int st = contour_count(ctx, field, grid, values, c);
+		if (st != UP_OK) return st;
+		const uint32_t V = c.ncells, T = 2 * c.nquads;
+		float *pos = (float *)buf(ctx, B_BASE_POS, (size_t)V * 12);
+		float *nrm = mesh->normals ? (float *)buf(ctx, B_BASE_NRM, (size_t)V * 12) : nullptr;
+		uint32_t *idx = (uint32_t *)buf(ctx, B_BASE_IDX, (size_t)T * 12);
+		contour_geometry(ctx, field, c, pos, nrm, idx);
+		MeshFilterArgs a{};
+		a.V = V;
+		a.T = T;
+		a.pos = pos;
+		a.nrm = nrm;
+		a.idx = idx;
+		if (field == UP_FIELD_WATER) {
+			float *elev = (float *)buf(ctx, B_BASE_ELEV, (size_t)V * 4);
+			// elevationRaw at the vertices; a NaN compares false and leaves the vertex invalid
+			check(launch_modes_points(ctx->d_modes, UP_FIELD_ELEVATION_RAW, pos, V, elev, nullptr, ctx->d_flag, ctx->stream), "elevation kernel");
+			a.elev = elev;
+		}
+		a.parent = (uint32_t *)buf(ctx, B_BASE_PARENT, (size_t)V * 4);
+		a.label = (uint32_t *)buf(ctx, B_BASE_LABEL, (size_t)V * 4);
+		a.cnt = (uint32_t *)buf(ctx, B_BASE_CNT, (size_t)V * 4);
+		a.newidx = (uint32_t *)buf(ctx, B_BASE_NEWIDX, (size_t)V * 4);
+		a.blk = (uint32_t *)buf(ctx, B_BASE_BLK, dc_scan_words(mesh_blocks(V, T)) * 4);
+		uint32_t *small = (uint32_t *)buf(ctx, B_BASE_SMALL, 64);
+		a.totals = small;
+		a.err = small + 4;
+		a.best = (unsigned long long *)(small + 8);
+		a.keep_v = (uint8_t *)buf(ctx, B_BASE_KEEPV, V);
+		a.valid2 = (uint8_t *)buf(ctx, B_BASE_VALID2, V);
+		a.keep_t = (uint8_t *)buf(ctx, B_BASE_KEEPT, T);
+		check(cudaMemsetAsync(a.err, 0, 4, ctx->stream), "cudaMemsetAsync");
+		check(mesh_filter(a, ctx->stream), "mesh filter kernels");
+		uint32_t tot[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+		check(cudaMemcpyAsync(tot, small, 32, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync totals");
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		if (tot[4]) return fail(ctx, UP_ERR_CUDA, "connected components: iteration limit reached");
+		const uint32_t nv = tot[0], nt = tot[1];
+		mesh->vertex_count = nv;
+		mesh->index_count = 3ull * nt;
+		if (nt == 0) return fail(ctx, UP_ERR_EMPTY_MESH, std::string("generated empty base ") + field_word(field) + " mesh");
+		if (!mesh->positions || !mesh->indices || mesh->vertex_capacity < nv || mesh->index_capacity < 3ull * nt)
+			return fail(ctx, UP_ERR_CAPACITY, "mesh buffers too small");
+		float *po = (float *)stage_out(ctx, B_MESH_POS, mesh->positions, (size_t)nv * 12);
+		float *no = (float *)stage_out(ctx, B_MESH_NRM, mesh->normals, (size_t)nv * 12);
+		uint32_t *io = (uint32_t *)stage_out(ctx, B_MESH_IDX, mesh->indices, (size_t)nt * 12);
+		check(mesh_compact(a, po, no, io, ctx->stream), "mesh compaction kernels");
+		finish_out(ctx, mesh->positions, po, (size_t)nv * 12);
+		finish_out(ctx, mesh->normals, no, (size_t)nv * 12);
+		finish_out(ctx, mesh->indices, io, (size_t)nt * 12);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_image_special_to_gltf_pbr(up_context *ctx, const uint8_t *special, uint32_t width, uint32_t height, uint8_t *pbr) {
+	if (!ctx || !special || !pbr || width == 0 || height == 0) return UP_ERR_INVALID_ARGUMENT;
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const size_t n = (size_t)width * height;
+		const uint8_t *si = (const uint8_t *)stage_in(ctx, B_IN0, special, n * 2);
+		uint8_t *po = (uint8_t *)stage_out(ctx, B_OUT0, pbr, n * 3);
+		check(image_pbr_run(si, width, height, po, ctx->stream), "pbr kernel");
+		finish_out(ctx, pbr, po, n * 3);
+		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+		return (int)UP_OK;
+	});
+}
+
+int up_image_height_to_normal(up_context *ctx, const uint8_t *height_map, uint32_t width, uint32_t height, float strength, uint8_t *normal) {
+	if (!ctx || !height_map || !normal || width == 0 || height == 0 || !(strength == strength)) return UP_ERR_INVALID_ARGUMENT;
+	return guarded(ctx, [&]() {
+		set_device(ctx);
+		const size_t n = (size_t)width * height;
+		const uint8_t *hi = (const uint8_t *)stage_in(ctx, B_IN0, height_map, n);
+		uint8_t *no = (uint8_t *)stage_out(ctx, B_OUT0, normal, n * 3);
+		check(image_normal_run(hi, width, height, strength, no, ctx->stream), "normal-map kernel");
+		finish_out(ctx, normal, no, n * 3);
 		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
 		return (int)UP_OK;
 	});

@@ -57,6 +57,29 @@ cudaError_t dc_geometry_synth(const up_synth_program &P, const float *d, const G
 cudaError_t dc_geometry_modes(const ModesDesc *M, int field, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells,
 	uint32_t nedges, uint32_t nquads, float *pos, float *nrm, uint32_t *idx, cudaStream_t s);
 
+// ---- mesh hygiene (up_mesh.cu)
+struct MeshFilterArgs {
+	uint32_t V, T;                 // vertices, triangles
+	const float *pos, *nrm;        // device; nrm may be null
+	const uint32_t *idx;           // device, 3 T
+	const float *elev;             // water: elevationRaw at the vertices; null for land/navigation
+	uint32_t *parent, *label, *cnt, *newidx; // V each
+	uint32_t *blk, *totals;        // dc_scan_words(mesh_blocks(V, T)), 4
+	unsigned long long *best;      // 1
+	uint8_t *keep_v, *valid2;      // V each
+	uint8_t *keep_t;               // T
+	unsigned *err;                 // union-find iteration limit flag
+};
+uint32_t mesh_blocks(uint32_t V, uint32_t T);
+// keep flags and their counts: totals[0] = kept vertices, totals[1] = kept triangles
+cudaError_t mesh_filter(const MeshFilterArgs &a, cudaStream_t s);
+// ordered compaction into device outputs (after mesh_filter)
+cudaError_t mesh_compact(const MeshFilterArgs &a, float *pos_out, float *nrm_out, uint32_t *idx_out, cudaStream_t s);
+
+// ---- texture post-processing (up_image.cu)
+cudaError_t image_pbr_run(const uint8_t *special, uint32_t W, uint32_t H, uint8_t *pbr, cudaStream_t s);
+cudaError_t image_normal_run(const uint8_t *height, uint32_t W, uint32_t H, float strength, uint8_t *normal, cudaStream_t s);
+
 // occupancy-derived persistent grid size
 int persistent_blocks(const void *kernel, int threads, size_t smem = 0);
 
