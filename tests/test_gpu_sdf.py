@@ -47,6 +47,30 @@ def test_grid_value_and_gradient(cuda, up, O, which):
     assert np.abs(d2 - ref).max() <= 1e-5
 
 
+@pytest.mark.parametrize("which", ["c1", "c2"])
+def test_grid_unaligned_device_outputs(cuda, up, O, which):
+    """Sample counts that are not a multiple of 4 (gradient planes off 16-byte
+    boundaries) and device outputs starting one float into an allocation:
+    the grid kernels' vector stores must fall back to scalar stores. (An even
+    nx keeps the x = 0 plane, where samples fall on noise lattice points and
+    ridged octaves have a gradient kink, out of the grid.)"""
+    torch = cuda
+    W = workloads()
+    P, spec = _programs()[which]
+    g = W.grid(spec, n=(42, 35, 33))
+    n = g.count
+    assert n % 4 != 0
+    planet = up.Planet(program=P)
+    dbuf = torch.zeros(n + 1, device="cuda")
+    gbuf = torch.zeros(3 * n + 1, device="cuda")
+    d, gr = dbuf[1:], gbuf[1:]
+    planet.sdf_grid(g, 1, outs=[d, None, None], grad=gr)
+    ref, rg = O.synth_points(P, O.grid_positions(g), grad=True)
+    assert np.abs(d.cpu().numpy() - ref).max() <= 1e-5
+    assert grad_ok(gr.cpu().numpy().reshape(3, n).T, rg)
+    assert float(dbuf[0]) == 0.0 and float(gbuf[0]) == 0.0
+
+
 def test_points_host_and_device_buffers(cuda, up, O):
     torch = cuda
     W = workloads()
@@ -96,3 +120,33 @@ def test_invalid_arguments(cuda, up):
     with pytest.raises(up.UpError) as e:
         planet.sdf_grid(g, 1)
     assert e.value.status == up.abi.UP_ERR_INVALID_ARGUMENT
+
+
+def test_host_outputs_pipelined_equal_device(cuda, up):
+    """up_sdf_grid into host memory runs in z-slabs with the device-to-host
+    copies overlapped; the values and gradients are the single launch's, bit
+    for bit (ragged last slab: 157 planes)."""
+    torch = cuda
+    W = workloads()
+    P = W.torus_spheres_ridged_cellular()
+    g = W.grid(W.GRID_C2, n=(161, 170, 157))
+    planet = up.Planet(program=P)
+    n = g.count
+    dd = torch.empty(n, device="cuda")
+    gd = torch.empty(3 * n, device="cuda")
+    planet.sdf_grid(g, 1, outs=[dd, None, None], grad=gd)
+    dh = np.empty(n, np.float32)
+    gh = np.empty(3 * n, np.float32)
+    planet.sdf_grid(g, 1, outs=[dh, None, None], grad=gh)
+    assert np.array_equal(dh, dd.cpu().numpy()) and np.array_equal(gh, gd.cpu().numpy())
+    pinned = torch.empty(n, pin_memory=True)
+    planet.sdf_grid(g, 1, outs=[pinned, None, None])
+    assert np.array_equal(pinned.numpy(), dh)
+    # reference modes, three fields in one pass
+    mp = up.Planet("sphere", "lakes", "default", seed=2)
+    gm = up.abi.Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), (170, 161, 163))
+    dev = [torch.empty(gm.count, device="cuda") for _ in range(3)]
+    mp.sdf_grid(gm, 7, outs=dev)
+    host = mp.sdf_grid(gm, 7)
+    for a, b in zip(host, dev):
+        assert np.array_equal(a, b.cpu().numpy())

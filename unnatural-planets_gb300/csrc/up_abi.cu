@@ -40,7 +40,7 @@ enum BufSlot {
 	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
 	B_BASE_POS, B_BASE_NRM, B_BASE_IDX, B_BASE_ELEV, B_BASE_PARENT, B_BASE_LABEL, B_BASE_CNT, B_BASE_NEWIDX, B_BASE_BLK, B_BASE_SMALL,
-	B_BASE_KEEPV, B_BASE_VALID2, B_BASE_KEEPT,
+	B_BASE_KEEPV, B_BASE_VALID2, B_BASE_KEEPT, B_PIPE0, B_PIPE1,
 	B_COUNT
 };
 
@@ -57,6 +57,10 @@ struct up_context {
 	unsigned *d_flag = nullptr;
 	struct Buf { void *p = nullptr; size_t n = 0; } bufs[B_COUNT];
 	void *batch = nullptr; // planned batch (up_batch.cu)
+	// device-to-host pipeline of up_sdf_grid: copies of slab k overlap the
+	// sampling of slab k + 1 (created on first use)
+	cudaStream_t copy_stream = nullptr;
+	cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -242,6 +246,72 @@ void contour_geometry(up_context *ctx, int field, ContourRun &c, float *pos, flo
 	else check(dc_geometry_modes(ctx->d_modes, field, c.d, c.g, S, c.ncells, c.nedges, c.nquads, pos, nrm, idx, ctx->stream), "contour geometry");
 }
 
+// up_sdf_grid into host memory, pipelined: the grid is sampled in z-slabs
+// into two device staging buffers (fields then gradient planes of the slab);
+// the copy stream moves slab k to the host while the caller's stream samples
+// slab k + 1. Slab coordinates use the full grid's index (GridDev::k0), so
+// values are bit-identical to the single launch.
+constexpr size_t GRID_PIPE_MIN = (size_t)1 << 22; // samples
+constexpr int GRID_PIPE_SLABS = 8;
+int sdf_grid_pipelined(up_context *ctx, uint32_t mask, const GridDev &g, float *const out[3], float *grad) {
+	if (!ctx->copy_stream) {
+		check(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+		for (int b = 0; b < 2; b++) {
+			check(cudaEventCreateWithFlags(&ctx->ev_done[b], cudaEventDisableTiming), "cudaEventCreate");
+			check(cudaEventCreateWithFlags(&ctx->ev_copied[b], cudaEventDisableTiming), "cudaEventCreate");
+		}
+	}
+	const uint32_t nz = g.n[2];
+	const size_t plane = (size_t)g.n[0] * g.n[1];
+	const size_t n = plane * nz;
+	const uint32_t sz = (nz + GRID_PIPE_SLABS - 1) / GRID_PIPE_SLABS;
+	int nf = 0;
+	for (int f = 0; f < 3; f++) nf += (int)(mask >> f & 1u);
+	const int nplanes = nf + (grad ? 3 : 0);
+	float *stage[2];
+	for (int b = 0; b < 2; b++) stage[b] = (float *)buf(ctx, B_PIPE0 + b, plane * sz * nplanes * 4);
+	reset_flag(ctx);
+	// the copy stream starts after work already queued on the caller's stream
+	check(cudaEventRecord(ctx->ev_copied[0], ctx->stream), "cudaEventRecord");
+	check(cudaEventRecord(ctx->ev_copied[1], ctx->stream), "cudaEventRecord");
+	int slab = 0;
+	for (uint32_t z0 = 0; z0 < nz; z0 += sz, slab++) {
+		const int b = slab & 1;
+		const uint32_t cz = nz - z0 < sz ? nz - z0 : sz;
+		const size_t cn = plane * cz;
+		GridDev gs = g;
+		gs.n[2] = cz;
+		gs.k0 = z0;
+		// buffer b is free once its previous slab's copies are done
+		check(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[b], 0), "cudaStreamWaitEvent");
+		float *o[3] = {nullptr, nullptr, nullptr};
+		int q = 0;
+		for (int f = 0; f < 3; f++)
+			if (mask >> f & 1u) o[f] = stage[b] + (size_t)(q++) * cn;
+		float *dg = grad ? stage[b] + (size_t)nf * cn : nullptr;
+		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, gs, o[0], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		else check(launch_modes_grid(ctx->d_modes, mask, gs, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		check(cudaEventRecord(ctx->ev_done[b], ctx->stream), "cudaEventRecord");
+		check(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_done[b], 0), "cudaStreamWaitEvent");
+		const size_t off = plane * z0;
+		for (int f = 0; f < 3; f++)
+			if (mask >> f & 1u)
+				check(cudaMemcpyAsync(out[f] + off, o[f], cn * 4, cudaMemcpyDeviceToHost, ctx->copy_stream), "cudaMemcpyAsync D2H");
+		for (int a = 0; grad && a < 3; a++)
+			check(cudaMemcpyAsync(grad + (size_t)a * n + off, dg + (size_t)a * cn, cn * 4, cudaMemcpyDeviceToHost, ctx->copy_stream),
+				"cudaMemcpyAsync D2H");
+		check(cudaEventRecord(ctx->ev_copied[b], ctx->copy_stream), "cudaEventRecord");
+	}
+	// the call completes with the last copies
+	check(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[(slab - 1) & 1], 0), "cudaStreamWaitEvent");
+	if (read_flag(ctx)) {
+		int f = 0;
+		while (!(mask >> f & 1u)) f++;
+		return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(f) + " sdf value");
+	}
+	return (int)UP_OK;
+}
+
 } // namespace
 
 // ============================================================================
@@ -335,6 +405,14 @@ int up_context_destroy(up_context *ctx) {
 	if (ctx->d_flag) cudaFree(ctx->d_flag);
 	if (ctx->d_modes) cudaFree(ctx->d_modes);
 	if (ctx->batch) batch_state_free(ctx->batch);
+	if (ctx->copy_stream) {
+		cudaStreamSynchronize(ctx->copy_stream);
+		cudaStreamDestroy(ctx->copy_stream);
+	}
+	for (int b = 0; b < 2; b++) {
+		if (ctx->ev_done[b]) cudaEventDestroy(ctx->ev_done[b]);
+		if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
+	}
 	delete ctx;
 	return UP_OK;
 }
@@ -419,6 +497,11 @@ int up_sdf_grid(up_context *ctx, uint32_t mask, const up_grid *grid, float *cons
 		set_device(ctx);
 		const GridDev g = make_grid(*grid);
 		const size_t n = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
+		// every output in host memory and a grid large enough: pipelined slabs
+		bool host_only = n >= GRID_PIPE_MIN && !(grad && is_device(grad));
+		for (int f = 0; f < 3; f++)
+			if ((mask >> f & 1u) && is_device(out[f])) host_only = false;
+		if (host_only) return sdf_grid_pipelined(ctx, mask, g, out, grad);
 		float *o[3] = {nullptr, nullptr, nullptr};
 		for (int f = 0; f < 3; f++)
 			if (mask >> f & 1u) o[f] = (float *)stage_out(ctx, B_OUT0 + f, out[f], n * 4);

@@ -11,6 +11,7 @@ namespace up {
 struct GridDev {
 	float lo[3], step[3];
 	uint32_t n[3];
+	uint32_t k0 = 0; // z index of the first plane (sampling of z-slabs of a larger grid)
 };
 GridDev make_grid(const up_grid &g);
 

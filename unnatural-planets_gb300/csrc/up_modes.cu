@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(128) modes_grid_kernel(const ModesDesc *__rest
 	bool bad = false;
 	for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
 		const uint32_t i = idx % nx, r = idx / nx, j = r % ny, k = r / ny;
-		const V3f p = v3(mgrid_coord(g, 0, i), mgrid_coord(g, 1, j), mgrid_coord(g, 2, k));
+		const V3f p = v3(mgrid_coord(g, 0, i), mgrid_coord(g, 1, j), mgrid_coord(g, 2, k + g.k0));
 		float v[3];
 		if (GRAD) {
 			Df f[3];

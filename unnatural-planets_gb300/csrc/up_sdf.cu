@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 	bool bad = false;
 	for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
 		const uint32_t i = idx % nx, r = idx / nx, j = r % ny, k = r / ny;
-		const V3f p = v3(grid_coord(g, 0, i), grid_coord(g, 1, j), grid_coord(g, 2, k));
+		const V3f p = v3(grid_coord(g, 0, i), grid_coord(g, 1, j), grid_coord(g, 2, k + g.k0));
 		const NG d = synth_eval<GRAD, T0, T1>(P, p);
 		out[idx] = d.v;
 		if (GRAD) {
@@ -91,11 +91,16 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 		const uint32_t j = row % ny, k = row / ny;
 		rc.i0 = run * R;
 		rc.py = grid_coord(g, 1, j);
-		rc.pz = grid_coord(g, 2, k);
+		rc.pz = grid_coord(g, 2, k + g.k0);
 		synth_run<GRAD, T0, T1>(P, rc, R, acc, RUNS_T);
 		if (!live) continue;
 		const uint64_t base = (uint64_t)row * nx + rc.i0;
-		const bool vec = rc.i0 + R <= nx && (base & 3) == 0;
+		// 16-byte stores only where every destination address is 16-byte
+		// aligned (caller pointers and plane offsets need not be)
+		const bool full = rc.i0 + R <= nx;
+		const bool vec = full && ((uintptr_t)(out + base) & 15) == 0;
+		const bool vecg = GRAD && full &&
+			(((uintptr_t)(grad + base) | (uintptr_t)(grad + plane + base) | (uintptr_t)(grad + 2 * plane + base)) & 15) == 0;
 		#pragma unroll 1
 		for (int r = 0; r < R; r += 4) {
 			float v[4], gx[4], gy[4], gz[4];
@@ -111,22 +116,25 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 			}
 			if (vec) {
 				*(float4 *)(out + base + r) = make_float4(v[0], v[1], v[2], v[3]);
-				if (GRAD) {
-					*(float4 *)(grad + base + r) = make_float4(gx[0], gx[1], gx[2], gx[3]);
-					*(float4 *)(grad + plane + base + r) = make_float4(gy[0], gy[1], gy[2], gy[3]);
-					*(float4 *)(grad + 2 * plane + base + r) = make_float4(gz[0], gz[1], gz[2], gz[3]);
-				}
 			} else {
 				#pragma unroll
 				for (int q = 0; q < 4; q++)
-					if (rc.i0 + r + q < nx) {
-						out[base + r + q] = v[q];
-						if (GRAD) {
+					if (rc.i0 + r + q < nx) out[base + r + q] = v[q];
+			}
+			if (GRAD) {
+				if (vecg) {
+					*(float4 *)(grad + base + r) = make_float4(gx[0], gx[1], gx[2], gx[3]);
+					*(float4 *)(grad + plane + base + r) = make_float4(gy[0], gy[1], gy[2], gy[3]);
+					*(float4 *)(grad + 2 * plane + base + r) = make_float4(gz[0], gz[1], gz[2], gz[3]);
+				} else {
+					#pragma unroll
+					for (int q = 0; q < 4; q++)
+						if (rc.i0 + r + q < nx) {
 							grad[base + r + q] = gx[q];
 							grad[plane + base + r + q] = gy[q];
 							grad[2 * plane + base + r + q] = gz[q];
 						}
-					}
+				}
 			}
 		}
 	}
