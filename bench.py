@@ -423,6 +423,15 @@ def run_ours(args) -> None:
         planet_step()
     planet_ms, planet_wall = timed(planet_step, args.steps)
 
+    # the same planet from the exactly sampled full grid (as the reference's
+    # marching cubes samples it): up_sdf_grid into device memory, then contour
+    def planet_full_step():
+        plain()
+        st = planet.lib.up_contour(planet.h, 0, C.byref(grid), C.c_void_p(d.data_ptr()), C.byref(mesh))
+        assert st == 0, st
+    planet_full_step()
+    planet_full_ms, _ = timed(planet_full_step, args.steps)
+
     # end to end through the C ABI with pinned host outputs (D2H inside the timed region)
     dh = torch.empty(N, pin_memory=True)
     gh = torch.empty(3 * N, pin_memory=True)
@@ -475,7 +484,11 @@ def run_ours(args) -> None:
                    "l2": "no inputs; 2.1 GB of outputs per step (> 129 MB L2)"},
         "plain_gsamples_s": ws * N / (t_plain * 1e-3) / 1e9, "plain_ms": t_plain,
         "ms_per_planet": sum(planet_ms) / len(planet_ms),
-        "planet": {"what": f"{args.grid}^3 value sampling + dual contouring (count, scan, emit, Hermite, QEF (FP32; FP64 near the truncation threshold), quads) into device buffers",
+        "ms_per_planet_full_grid": sum(planet_full_ms) / len(planet_full_ms),
+        "planet": {"what": f"{args.grid}^3 planet mesh into device buffers: up_contour samples the grid with the narrow band "
+                           "(noise evaluated where |base| <= noise bound + one grid step; the mesh is bit-identical to contouring "
+                           "the full grid), then dual contouring (signs, count, scan, emit, Hermite, QEF, quads); "
+                           "ms_per_planet_full_grid samples every point exactly first (up_sdf_grid) and contours those values",
                    "vertices": V, "triangles": I // 3},
         "e2e": {"value": ws * N / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 * N,
                 "what": "up_sdf_grid value+gradient into pinned host buffers"},

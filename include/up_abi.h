@@ -222,7 +222,10 @@ int up_sdf_grid(up_context *ctx, uint32_t fields_mask, const up_grid *grid, floa
 /* Dual contouring of one field: replaces MarchingCubes::makeMesh
  * (meshGeneration.cpp:40) and the flow of meshGenerateGeneric (:32-44).
  * Samples the field on grid (or takes it from values when not NULL: a
- * host or device array of nx*ny*nz floats), finds sign-change edges, places
+ * host or device array of nx*ny*nz floats; a synthetic context samples only
+ * a narrow band exactly: where |base| exceeds the bound of its noise layers
+ * plus one grid step, only the sign is needed and the base gives it, so the
+ * mesh equals the mesh of the fully sampled grid), finds sign-change edges, places
  * one vertex per active cell by a QEF solve on analytic Hermite normals
  * (FP32; FP64 for cells whose eigenvalue truncation is within FP32
  * rounding of the threshold), and emits two triangles per interior sign-change edge, wound so

@@ -109,6 +109,9 @@ void hc_synth_texel(const up_synth_program *P, const float *pos, uint64_t n, flo
 
 // whole grid of the torus/spheres/ridged-Perlin/cellular program through the
 // run-based evaluation (runs of RUN_R samples along x, the kernel's order)
+float hc_noise_bound(int type, int dist, int op) { return noise_abs_bound(type, dist, op); }
+float hc_synth_noise_bound(const up_synth_program *P) { return synth_noise_bound(*P); }
+
 void hc_grid_runs(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float *out, float *grad) {
 	constexpr int R = RUN_R;
 	constexpr int T1 = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);

@@ -31,6 +31,10 @@ def H():
     L.hc_corner_hash.restype = C.c_uint32
     L.hc_corner_hash.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int]
     L.hc_grid_runs.argtypes = [C.POINTER(abi.SynthProgram), vp, vp, vp, vp, vp]
+    L.hc_noise_bound.restype = C.c_float
+    L.hc_noise_bound.argtypes = [C.c_int, C.c_int, C.c_int]
+    L.hc_synth_noise_bound.restype = C.c_float
+    L.hc_synth_noise_bound.argtypes = [C.POINTER(abi.SynthProgram)]
     return L
 
 
@@ -110,3 +114,22 @@ def test_grid_runs_equal_per_sample(H, O, n):
     plain = np.empty(N, np.float32)
     H.hc_grid_runs(C.byref(P), lo.ctypes.data, st.ctypes.data, nn.ctypes.data, plain.ctypes.data, None)
     assert np.array_equal(plain, out)
+
+
+@pytest.mark.parametrize("t,dist,op", CASES)
+def test_noise_bound_holds(H, O, t, dist, op):
+    """The |n| bounds behind the narrow band of contouring (noise_abs_bound)
+    hold for the oracle's noise on many points, and are not vacuous."""
+    x = np.random.default_rng(100 + t * 31 + dist * 7 + op).uniform(-50, 50, size=(200000, 3))
+    v = O.noise(dict(type=t, seed=3, distance=dist, operation=op), x)
+    b = H.hc_noise_bound(t, dist, op)
+    assert np.abs(v).max() <= b
+    assert np.abs(v).max() >= 0.1 * b
+
+
+def test_synth_noise_bound(H, O):
+    W = workloads()
+    P = W.torus_spheres_ridged_cellular()
+    # ridged Perlin: |1 - 2|n|| <= 3 per unit amplitude; cellular F2 - F1 - 1 <= sqrt(6) - 1
+    want = 0.04 * 3.0 + 0.02 * (6 ** 0.5 - 1)
+    assert abs(H.hc_synth_noise_bound(C.byref(P)) - want) <= 1e-6

@@ -68,3 +68,32 @@ def test_capacity_and_empty(cuda, up):
     st = planet.lib.up_contour(planet.h, 0, C.byref(far), None, C.byref(m))
     assert st == up.abi.UP_ERR_EMPTY_MESH
     assert b"empty" in planet.lib.up_last_error(planet.h)
+
+
+def _band_programs():
+    W = workloads()
+    rng = np.random.default_rng(12)
+    progs = [("c1", W.sphere_fbm(), W.grid(W.GRID_C1, n=(96, 90, 84))),
+             ("c2", W.torus_spheres_ridged_cellular(), W.grid(W.GRID_C2, n=(128, 120, 112)))]
+    for i in range(3):
+        P = W.mixed_planet(rng)
+        P.layer[0].amp[0] = 0.3  # a wide band
+        progs.append((f"mixed{i}", P, W.grid(dict(lo=(-1.6, -1.6, -1.6), hi=(1.6, 1.6, 1.6), n=(80, 80, 80)))))
+    return progs
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_narrow_band_contour_equals_full_grid(cuda, up, k):
+    """up_contour samples its grid with the narrow band (noise skipped where
+    |base| exceeds the noise bound plus one grid step); contouring the exactly
+    sampled grid passed in as values gives the same mesh bit for bit, and so
+    does the base mesh."""
+    name, P, g = _band_programs()[k]
+    planet = up.Planet(program=P)
+    full = planet.sdf_grid(g, 1)[0]
+    banded = planet.contour(g)
+    exact = planet.contour(g, values=full)
+    for a, b in zip(banded, exact):
+        assert np.array_equal(a, b), name
+    for a, b in zip(planet.mesh_generate_base(g), planet.mesh_generate_base(g, values=full)):
+        assert np.array_equal(a, b), name

@@ -4,8 +4,10 @@
 #include "up_internal.h"
 #include "up_modes_desc.h"
 #include "up_noise.cuh"
+#include "up_synth.cuh"
 
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -199,6 +201,21 @@ struct ContourRun {
 	DcScratch S{};
 	uint32_t ncells = 0, nedges = 0, nquads = 0;
 };
+// Narrow band of contouring for a synthetic program. |layers| <= B everywhere
+// (synth_noise_bound) and the base is 1-Lipschitz (exact SDFs and their
+// polynomial smooth union), so a sample with |base| > B + (longest grid step)
+// has the sign of the base, and so has every grid neighbour: it is neither an
+// end of a sign-change edge nor decides an active cell by anything but its
+// sign, and its value is not needed. The margins absorb FP32 rounding.
+// Returns 0 (sample everything exactly) when the bound is not finite.
+float contour_band(const up_synth_program &P, const GridDev &g) {
+	const float B = synth_noise_bound(P);
+	float st = g.step[0];
+	if (g.step[1] > st) st = g.step[1];
+	if (g.step[2] > st) st = g.step[2];
+	const float band = (B + st) * 1.001f + 1e-5f;
+	return std::isfinite(band) ? band : 0.f;
+}
 int contour_count(up_context *ctx, int field, const up_grid *grid, const float *values, ContourRun &c) {
 	c.g = make_grid(*grid);
 	const size_t np = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
@@ -208,7 +225,7 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 	} else {
 		float *gd = (float *)buf(ctx, B_GRID, np * 4);
 		reset_flag(ctx);
-		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream, contour_band(ctx->prog, c.g)), "sdf grid kernel");
 		else {
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;

@@ -309,14 +309,23 @@ UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename 
 	}
 }
 
-// one run: base shape plus layers into acc (R must be a multiple of CELL_SUB)
+// one run: base shape plus layers into acc (R must be a multiple of CELL_SUB).
+// band > 0: when every sample of the warp's task has |base| > band, the layers
+// are skipped and acc holds the base (the narrow band of contouring: such
+// samples have the sign of the base and are not ends of sign-change edges)
 template<bool GRAD, int T0, int T1>
-UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride) {
+UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride, float band = 0.f) {
+	bool far = band > 0.f;
 	#pragma unroll 1
 	for (int r = 0; r < R; r++) {
 		const NG b = synth_base<GRAD>(P, v3(rc.px(r), rc.py, rc.pz));
 		acc_set(acc, r * stride, b.v, b.g.x, b.g.y, b.g.z);
+		far = far && fabsf(b.v) > band;
 	}
+#ifdef __CUDA_ARCH__
+	far = __all_sync(0xFFFFFFFFu, far); // every lane of the warp runs every task
+#endif
+	if (far) return;
 	if (P.n_layers > 0) layer_run<GRAD, T0>(P.layer[0], rc, R, acc, stride);
 	if (P.n_layers > 1) layer_run<GRAD, T1>(P.layer[1], rc, R, acc, stride);
 }

@@ -19,7 +19,10 @@ GridDev make_grid(const up_grid &g);
 struct ModesDesc;
 
 // ---- SDF sampling (up_sdf.cu / up_modes.cu)
-cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s);
+// band > 0: narrow band of contouring (samples with |base| > band keep the
+// base value); 0: exact values everywhere
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s,
+	float band = 0.f);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 cudaError_t launch_modes_grid(const ModesDesc *M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag, cudaStream_t s);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);

@@ -37,9 +37,11 @@ __device__ __forceinline__ float grid_coord(const GridDev &g, int a, uint32_t i)
 	return __fadd_rn(__fmul_rn((float)i, g.step[a]), g.lo[a]);
 }
 
+// band > 0: samples with |base| > band take the base value (narrow band of
+// contouring, see synth_run)
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
-	float *__restrict__ grad, unsigned *__restrict__ nanflag) {
+	float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint64_t plane = (uint64_t)nx * ny * g.n[2];
 	const uint32_t total = (uint32_t)plane;
@@ -47,7 +49,13 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 	for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
 		const uint32_t i = idx % nx, r = idx / nx, j = r % ny, k = r / ny;
 		const V3f p = v3(grid_coord(g, 0, i), grid_coord(g, 1, j), grid_coord(g, 2, k + g.k0));
-		const NG d = synth_eval<GRAD, T0, T1>(P, p);
+		NG d;
+		if (band > 0.f) {
+			d = synth_base<GRAD>(P, p);
+			if (!(fabsf(d.v) > band)) d = synth_eval<GRAD, T0, T1>(P, p);
+		} else {
+			d = synth_eval<GRAD, T0, T1>(P, p);
+		}
 		out[idx] = d.v;
 		if (GRAD) {
 			grad[idx] = d.g.x;
@@ -65,7 +73,7 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 constexpr int RUNS_T = 128;
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
-	float *__restrict__ grad, unsigned *__restrict__ nanflag) {
+	float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
 	typedef typename AccOf<GRAD>::T A;
 	extern __shared__ __align__(16) unsigned char runs_smem[];
 	A *acc = (A *)runs_smem + threadIdx.x;
@@ -92,7 +100,7 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 		rc.i0 = run * R;
 		rc.py = grid_coord(g, 1, j);
 		rc.pz = grid_coord(g, 2, k + g.k0);
-		synth_run<GRAD, T0, T1>(P, rc, R, acc, RUNS_T);
+		synth_run<GRAD, T0, T1>(P, rc, R, acc, RUNS_T, band);
 		if (!live) continue;
 		const uint64_t base = (uint64_t)row * nx + rc.i0;
 		// 16-byte stores only where every destination address is 16-byte
@@ -194,22 +202,22 @@ static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, A... 
 	return cudaGetLastError();
 }
 
-cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s) {
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s, float band) {
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
 	const Spec sp = spec_of(P);
 	if (sp == SPEC_PERLIN_CELL) {
-		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag);
-		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag);
+		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag, band);
+		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag, band);
 	}
 	if (grad) {
-		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag);
-		if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<true, 3, -1>, n, s, P, g, out, grad, nanflag);
-		return launch_persistent(synth_grid_kernel<true, -1, -1>, n, s, P, g, out, grad, nanflag);
+		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag, band);
+		if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<true, 3, -1>, n, s, P, g, out, grad, nanflag, band);
+		return launch_persistent(synth_grid_kernel<true, -1, -1>, n, s, P, g, out, grad, nanflag, band);
 	}
-	if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<false, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag);
-	if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<false, 3, -1>, n, s, P, g, out, grad, nanflag);
-	return launch_persistent(synth_grid_kernel<false, -1, -1>, n, s, P, g, out, grad, nanflag);
+	if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<false, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag, band);
+	if (sp == SPEC_SIMPLEX) return launch_persistent(synth_grid_kernel<false, 3, -1>, n, s, P, g, out, grad, nanflag, band);
+	return launch_persistent(synth_grid_kernel<false, -1, -1>, n, s, P, g, out, grad, nanflag, band);
 }
 
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s) {

@@ -115,6 +115,51 @@ UP_HD NG synth_base(const up_synth_program &P, V3f p) {
 	}
 }
 
+// Upper bounds of |n| per noise type, from the definitions in up_noise.cuh:
+//  value: a convex combination of lattice values in [-1, 1) -> 1;
+//  cubic: 0.75 x (sum of |Catmull-Rom weights| <= 1 + t(1 - t) <= 1.25)^3;
+//  Perlin: a convex combination of g.d with g a 12-edge vector and the
+//    corner offsets in [-1, 1]^3, |g.d| <= 2;
+//  simplex: 4 corners x 76 max_r (0.5 - r^2)^4 sqrt(2) r (r^2 = 1/18) < 4;
+//  simplex-reduced: 4 x 31 max_r (0.5 - r^2)^3 sqrt(2) r (r^2 = 1/14) < 3.7;
+//  cellular: F1 <= the distance to the own cell's point (|v_a| < 1) and
+//    F2 <= the larger of that and the distance to a face neighbour's point
+//    (|v_a| < 2 on one axis, < 1 on the others): Euclidean sqrt(3) / sqrt(6),
+//    Manhattan 3 / 4, Hybrid 6 / 10; then the operation.
+UP_HD float noise_abs_bound(int type, int dist, int op) {
+	switch (type) {
+		case UP_NOISE_VALUE: return 1.f;
+		case UP_NOISE_CUBIC: return 0.75f * 1.953125f;
+		case UP_NOISE_PERLIN: return 2.f;
+		case UP_NOISE_SIMPLEX: return 4.f;
+		case UP_NOISE_SIMPLEX_REDUCED: return 3.7f;
+		default: {
+			const float f1 = dist == UP_DIST_EUCLIDEAN ? 1.7320509f : (dist == UP_DIST_MANHATTAN ? 3.f : 6.f);
+			const float f2 = dist == UP_DIST_EUCLIDEAN ? 2.4494898f : (dist == UP_DIST_MANHATTAN ? 4.f : 10.f);
+			float m = 1.f;
+			switch (op) {
+				case UP_OP_DISTANCE: m = f1 - 1.f; break;
+				case UP_OP_DISTANCE2: case UP_OP_SUBTRACT: m = f2 - 1.f; break;
+				case UP_OP_ADD: m = 0.5f * (f1 + f2) - 1.f; break;
+				case UP_OP_MULTIPLY: m = 0.5f * f1 * f2 - 1.f; break;
+				default: m = 1.f; break; // cell value, F1 / F2 - 1
+			}
+			return m > 1.f ? m : 1.f;
+		}
+	}
+}
+// |sum of the layers| <= this everywhere; NaN when a parameter is not finite
+UP_HD float synth_noise_bound(const up_synth_program &P) {
+	float b = 0.f;
+	for (int l = 0; l < P.n_layers; l++) {
+		const up_noise_layer &L = P.layer[l];
+		const float nm = noise_abs_bound(L.type, L.distance, L.operation);
+		const float sm = L.fractal == UP_FRACTAL_RIDGED ? (2.f * nm - 1.f > 1.f ? 2.f * nm - 1.f : 1.f) : nm;
+		for (int i = 0; i < L.octaves; i++) b += fabsf(L.amp[i]) * sm;
+	}
+	return b;
+}
+
 // full program; T0/T1 = compile-time noise type of layer 0/1 (-1 = runtime)
 template<bool GRAD, int T0, int T1>
 UP_HD NG synth_eval(const up_synth_program &P, V3f p) {
