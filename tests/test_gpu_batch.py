@@ -71,3 +71,15 @@ def test_batch_replay_writes_live_buffers(cuda, up):
     for k in first:
         assert np.array_equal(res[k], first[k]), k
     assert all((j == 7).all() for j in junk)
+
+
+def test_batch_narrow_band_equals_exact(cuda, up):
+    """Without a values buffer the batch samples its chunks with the narrow
+    band of contouring; the meshes equal those of the exact sampling."""
+    W = workloads()
+    planets, chunks = W.chunk_set(n_planets=6, n_chunks=40, seed=5, edge_lo=12, edge_hi=48)
+    ctx = up.Planet(program=planets[0])
+    exact = up.batch_run(ctx, planets, chunks, values=True)
+    banded = up.batch_run(ctx, planets, chunks, values=False)
+    for k in ("positions", "indices", "vertex_offsets", "index_offsets"):
+        assert np.array_equal(exact[k], banded[k]), k

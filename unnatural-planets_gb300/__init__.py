@@ -200,21 +200,25 @@ def batch_run(planet_or_lib, planets, chunks, values=False, device=False):
     Cs = (abi.Chunk * len(chunks))(*[abi.Chunk(p, g) for p, g in chunks])
     vo = np.zeros(len(chunks) + 1, np.uint64)
     io = np.zeros(len(chunks) + 1, np.uint64)
-    o = abi.BatchOut(None, None, 0, 0, vo.ctypes.data, io.ctypes.data, 0, 0, None, 0)
+    nval = sum(g.count for _, g in chunks)
+    if device:
+        import torch
+        val = torch.empty(nval, device="cuda") if values else None
+    else:
+        val = np.empty(nval, np.float32) if values else None
+    # the sizing call already names the values buffer: the library plans exact
+    # sampling when values are read and narrow-band sampling otherwise
+    o = abi.BatchOut(None, None, 0, 0, vo.ctypes.data, io.ctypes.data, 0, 0, _addr(val), nval if values else 0)
     st = ctx.lib.up_batch_run(ctx.h, P, len(planets), Cs, len(chunks), C.byref(o))
     if st != abi.UP_ERR_CAPACITY:
         ctx._check(st)
     V, I = int(o.vertex_count), int(o.index_count)
-    nval = sum(g.count for _, g in chunks)
     if device:
-        import torch
         pos = torch.empty((V, 3), device="cuda")
         idx = torch.empty(I, dtype=torch.int32, device="cuda")
-        val = torch.empty(nval, device="cuda") if values else None
     else:
         pos = np.empty((V, 3), np.float32)
         idx = np.empty(I, np.uint32)
-        val = np.empty(nval, np.float32) if values else None
     o = abi.BatchOut(_addr(pos), _addr(idx), V, I, vo.ctypes.data, io.ctypes.data, 0, 0, _addr(val), nval if values else 0)
     ctx._check(ctx.lib.up_batch_run(ctx.h, P, len(planets), Cs, len(chunks), C.byref(o)))
     # `o` holds raw addresses of vo/io and of the outputs: they stay referenced

@@ -29,7 +29,7 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 cudaError_t tiles_run(const ModesDesc *M, int purpose, const float *pos, const float *nrm, uint64_t n, float *out11, uint8_t *bt, cudaStream_t s);
 void batch_state_free(void *p);
 cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks,
-	uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
+	bool exact_values, uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
 	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, cudaStream_t caller);
 } // namespace up
 
@@ -201,21 +201,6 @@ struct ContourRun {
 	DcScratch S{};
 	uint32_t ncells = 0, nedges = 0, nquads = 0;
 };
-// Narrow band of contouring for a synthetic program. |layers| <= B everywhere
-// (synth_noise_bound) and the base is 1-Lipschitz (exact SDFs and their
-// polynomial smooth union), so a sample with |base| > B + (longest grid step)
-// has the sign of the base, and so has every grid neighbour: it is neither an
-// end of a sign-change edge nor decides an active cell by anything but its
-// sign, and its value is not needed. The margins absorb FP32 rounding.
-// Returns 0 (sample everything exactly) when the bound is not finite.
-float contour_band(const up_synth_program &P, const GridDev &g) {
-	const float B = synth_noise_bound(P);
-	float st = g.step[0];
-	if (g.step[1] > st) st = g.step[1];
-	if (g.step[2] > st) st = g.step[2];
-	const float band = (B + st) * 1.001f + 1e-5f;
-	return std::isfinite(band) ? band : 0.f;
-}
 int contour_count(up_context *ctx, int field, const up_grid *grid, const float *values, ContourRun &c) {
 	c.g = make_grid(*grid);
 	const size_t np = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
@@ -765,8 +750,8 @@ int up_batch_run(up_context *ctx, const up_synth_program *planets, size_t nplane
 		const uint32_t *didx = nullptr;
 		uint64_t nval = 0;
 		bool nan = false, replayed = false;
-		check(batch_execute(ctx->batch, planets, nplanets, chunks, nchunks, ncells, nquads, cc, cq, dpos, didx, dval, nval, nan, replayed,
-			ctx->stream), "batch kernels");
+		check(batch_execute(ctx->batch, planets, nplanets, chunks, nchunks, out->values != nullptr, ncells, nquads, cc, cq, dpos, didx, dval, nval,
+			nan, replayed, ctx->stream), "batch kernels");
 		if (nan) return fail(ctx, UP_ERR_NAN, "invalid land sdf value");
 		out->vertex_count = ncells;
 		out->index_count = 6ull * nquads;

@@ -32,6 +32,7 @@ struct BatchChunkDev {
 	GridDev g;
 	uint32_t planet;
 	uint32_t pt_off, cell_off, blk_off, tile_off;
+	float band; // narrow band of contouring (0: exact values, when the caller reads them)
 };
 
 constexpr uint32_t BATCH_TILE = 1024;
@@ -74,7 +75,9 @@ __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_pr
 			const uint32_t s = base + it;
 			if (s >= npts) break;
 			const uint32_t i = s % nx, r = s / nx, j = r % ny, k = r / ny;
-			const float v = synth_eval<false, -1, -1>(P, v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k))).v;
+			const V3f p = v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k));
+			float v = ch.band > 0.f ? synth_base<false>(P, p).v : 0.f;
+			if (!(ch.band > 0.f && fabsf(v) > ch.band)) v = synth_eval<false, -1, -1>(P, p).v;
 			d[ch.pt_off + s] = v;
 			bad |= isnan(v);
 		}
@@ -295,11 +298,12 @@ void batch_state_free(void *p) { delete (BatchState *)p; }
 // device outputs are in the state's pos/idx buffers and counts are filled.
 // Returns cudaSuccess or an error; *nan set when a sample was NaN.
 cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks,
-	uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
+	bool exact_values, uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
 	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, cudaStream_t caller) {
-	std::vector<uint8_t> key(nplanets * sizeof(up_synth_program) + nchunks * sizeof(up_chunk));
+	std::vector<uint8_t> key(nplanets * sizeof(up_synth_program) + nchunks * sizeof(up_chunk) + 1);
 	std::memcpy(key.data(), planets, nplanets * sizeof(up_synth_program));
 	std::memcpy(key.data() + nplanets * sizeof(up_synth_program), chunks, nchunks * sizeof(up_chunk));
+	key.back() = exact_values ? 1 : 0;
 	BatchState *S = (BatchState *)state;
 	cudaError_t e;
 	replayed = false;
@@ -329,6 +333,7 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 			BatchChunkDev &t = tab[c];
 			t.g = make_grid(chunks[c].grid);
 			t.planet = chunks[c].planet;
+			t.band = exact_values ? 0.f : contour_band(planets[t.planet], t.g);
 			const uint64_t n = (uint64_t)t.g.n[0] * t.g.n[1] * t.g.n[2];
 			t.pt_off = (uint32_t)pts;
 			t.cell_off = (uint32_t)cells;

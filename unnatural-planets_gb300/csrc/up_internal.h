@@ -23,6 +23,8 @@ struct ModesDesc;
 // base value); 0: exact values everywhere
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s,
 	float band = 0.f);
+// narrow band of contouring for program P on grid g (0 when unbounded)
+float contour_band(const up_synth_program &P, const GridDev &g);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 cudaError_t launch_modes_grid(const ModesDesc *M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag, cudaStream_t s);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);

@@ -10,6 +10,7 @@
 #include "up_internal.h"
 #include "up_synth.cuh"
 #include "up_grid_runs.cuh"
+#include <cmath>
 
 #include <mutex>
 
@@ -202,6 +203,21 @@ static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, A... 
 	return cudaGetLastError();
 }
 
+// Narrow band of contouring for a synthetic program. |layers| <= B everywhere
+// (synth_noise_bound) and the base is 1-Lipschitz (exact SDFs and their
+// polynomial smooth union), so a sample with |base| > B + (longest grid step)
+// has the sign of the base, and so has every grid neighbour: it is neither an
+// end of a sign-change edge nor decides an active cell by anything but its
+// sign, and its value is not needed. The margins absorb FP32 rounding.
+// Returns 0 (sample everything exactly) when the bound is not finite.
+float contour_band(const up_synth_program &P, const GridDev &g) {
+	const float B = synth_noise_bound(P);
+	float st = g.step[0];
+	if (g.step[1] > st) st = g.step[1];
+	if (g.step[2] > st) st = g.step[2];
+	const float band = (B + st) * 1.001f + 1e-5f;
+	return std::isfinite(band) ? band : 0.f;
+}
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s, float band) {
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
