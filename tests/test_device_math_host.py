@@ -130,6 +130,6 @@ def test_noise_bound_holds(H, O, t, dist, op):
 def test_synth_noise_bound(H, O):
     W = workloads()
     P = W.torus_spheres_ridged_cellular()
-    # ridged Perlin: |1 - 2|n|| <= 3 per unit amplitude; cellular F2 - F1 - 1 <= sqrt(6) - 1
-    want = 0.04 * 3.0 + 0.02 * (6 ** 0.5 - 1)
+    # ridged Perlin: |1 - 2|n|| <= 2 * 1.1 - 1 per unit amplitude; cellular F2 - F1 - 1 <= sqrt(6) - 1
+    want = 0.04 * 1.2 + 0.02 * (6 ** 0.5 - 1)
     assert abs(H.hc_synth_noise_bound(C.byref(P)) - want) <= 1e-6

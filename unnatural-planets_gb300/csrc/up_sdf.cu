@@ -69,8 +69,10 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 }
 
 // x-coherent runs (up_grid_runs.cuh): a warp task is RUN_R consecutive x
-// samples of 32 rows; accumulators in dynamic shared memory, RUNS_T slots
-// per sample index, so thread t owns acc[r * RUNS_T + t]
+// samples of 32 rows, the rows an 8 (y) x 4 (z) tile (a compact task skips the
+// noise more often under the narrow band of contouring); accumulators in
+// dynamic shared memory, RUNS_T slots per sample index, so thread t owns
+// acc[r * RUNS_T + t]
 constexpr int RUNS_T = 128;
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
@@ -80,9 +82,11 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 	A *acc = (A *)runs_smem + threadIdx.x;
 	constexpr int R = RUN_R;
 	const uint32_t nx = g.n[0], ny = g.n[1];
-	const uint32_t nrows = ny * g.n[2];
+	const uint32_t nz = g.n[2];
+	const uint32_t nrows = ny * nz;
 	const uint32_t nruns = (nx + R - 1) / R;
-	const uint64_t ntasks = (uint64_t)nruns * ((nrows + 31) / 32);
+	const uint32_t tny = (ny + 7) / 8, tnz = (nz + 3) / 4;
+	const uint64_t ntasks = (uint64_t)nruns * tny * tnz;
 	const uint64_t plane = (uint64_t)nx * nrows;
 	const uint32_t lane = threadIdx.x & 31;
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -93,11 +97,11 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 	rc.nx = nx;
 	bool bad = false;
 	for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nwarps) {
-		const uint32_t run = (uint32_t)(t % nruns), grp = (uint32_t)(t / nruns);
-		const uint32_t row_raw = grp * 32 + lane;
-		const bool live = row_raw < nrows;
-		const uint32_t row = live ? row_raw : nrows - 1;
-		const uint32_t j = row % ny, k = row / ny;
+		const uint32_t run = (uint32_t)(t % nruns), tile = (uint32_t)(t / nruns);
+		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
+		const bool live = jr < ny && kr < nz;
+		const uint32_t j = jr < ny ? jr : ny - 1, k = kr < nz ? kr : nz - 1;
+		const uint32_t row = k * ny + j;
 		rc.i0 = run * R;
 		rc.py = grid_coord(g, 1, j);
 		rc.pz = grid_coord(g, 2, k + g.k0);
@@ -196,7 +200,7 @@ static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, A... 
 	constexpr size_t smem = (size_t)RUN_R * RUNS_T * sizeof(typename AccOf<GRAD>::T);
 	static_assert(smem <= 48 * 1024, "runs accumulators exceed the default shared-memory limit");
 	uint64_t blocks = (uint64_t)persistent_blocks((const void *)kernel, RUNS_T, smem);
-	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] * g.n[2] + 31) / 32);
+	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
 	const uint64_t need = (tasks + RUNS_T / 32 - 1) / (RUNS_T / 32);
 	if (blocks > need) blocks = need > 0 ? need : 1;
 	kernel<<<(unsigned)blocks, RUNS_T, smem, s>>>(args...);

@@ -118,10 +118,13 @@ UP_HD NG synth_base(const up_synth_program &P, V3f p) {
 // Upper bounds of |n| per noise type, from the definitions in up_noise.cuh:
 //  value: a convex combination of lattice values in [-1, 1) -> 1;
 //  cubic: 0.75 x (sum of |Catmull-Rom weights| <= 1 + t(1 - t) <= 1.25)^3;
-//  Perlin: a convex combination of g.d with g a 12-edge vector and the
-//    corner offsets in [-1, 1]^3, |g.d| <= 2;
-//  simplex: 4 corners x 76 max_r (0.5 - r^2)^4 sqrt(2) r (r^2 = 1/18) < 4;
-//  simplex-reduced: 4 x 31 max_r (0.5 - r^2)^3 sqrt(2) r (r^2 = 1/14) < 3.7;
+//  Perlin, simplex, simplex-reduced: |g.d| <= max over axis pairs of
+//    |d_a| + |d_b| for a 12-edge gradient g, so |n| <= M(p) = sum over the
+//    corners of weight x that maximum; M's maximum over the cell (Perlin:
+//    trilinear quintic weights, 1.037; simplex: 76 (0.5 - r^2)^4, 0.989;
+//    reduced: 31 (0.5 - r^2)^3, 0.992, found on dense grids of the cell with
+//    a Lipschitz margin, recomputed by tests/test_noise_bounds.py) is below
+//    1.1 for all three;
 //  cellular: F1 <= the distance to the own cell's point (|v_a| < 1) and
 //    F2 <= the larger of that and the distance to a face neighbour's point
 //    (|v_a| < 2 on one axis, < 1 on the others): Euclidean sqrt(3) / sqrt(6),
@@ -130,9 +133,9 @@ UP_HD float noise_abs_bound(int type, int dist, int op) {
 	switch (type) {
 		case UP_NOISE_VALUE: return 1.f;
 		case UP_NOISE_CUBIC: return 0.75f * 1.953125f;
-		case UP_NOISE_PERLIN: return 2.f;
-		case UP_NOISE_SIMPLEX: return 4.f;
-		case UP_NOISE_SIMPLEX_REDUCED: return 3.7f;
+		case UP_NOISE_PERLIN: return 1.1f;
+		case UP_NOISE_SIMPLEX: return 1.1f;
+		case UP_NOISE_SIMPLEX_REDUCED: return 1.1f;
 		default: {
 			const float f1 = dist == UP_DIST_EUCLIDEAN ? 1.7320509f : (dist == UP_DIST_MANHATTAN ? 3.f : 6.f);
 			const float f2 = dist == UP_DIST_EUCLIDEAN ? 2.4494898f : (dist == UP_DIST_MANHATTAN ? 4.f : 10.f);
