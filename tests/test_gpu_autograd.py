@@ -54,3 +54,23 @@ def test_inverse_fit_recovers_parameters(cuda, up):
         opt.step()
         first = first if first is not None else float(loss.detach())
     assert float(loss.detach()) < 0.05 * first
+
+
+def test_gradcheck_4096_points(cuda, up):
+    """torch.autograd.gradcheck of L(theta) = mean(d(x; theta)^2) on 4096
+    seeded shell points of the sphere - 4-octave simplex FBM planet (smooth in
+    theta). The SDF computes in FP32, so the finite differences use a large
+    step and tolerances set for FP32 rounding."""
+    torch = cuda
+    AG = importlib.import_module("unnatural-planets_gb300.autograd")
+    W = workloads()
+    P = W.sphere_fbm()
+    planet = up.Planet(program=P)
+    x = torch.from_numpy(W.shell_points(1.0, 0.05, 4096, seed=13)).cuda()
+    theta = torch.from_numpy(W.theta_of(P)).cuda().requires_grad_(True)
+
+    def loss(t):
+        d = AG.sdf(t, x, planet)
+        return (d.double() ** 2).mean()
+
+    assert torch.autograd.gradcheck(loss, (theta,), eps=2e-3, atol=2e-5, rtol=2e-2, nondet_tol=1e-6, fast_mode=False)
