@@ -74,6 +74,26 @@ UP_HD V3f grad_lookup(uint32_t h) {
 #endif
 }
 
+// Per-warp table of the x quantities of one lattice octave: every lane of a
+// warp shares the run's x coordinates, so lanes 0..R-1 fill entry r = lane
+// once per octave and all lanes read it (shared-memory broadcast) instead of
+// each forming x, floor, fade and fade' per sample.
+struct XTab { float fx, u, du; int cx; };
+constexpr int RUNS_WARPS = 4; // warps per block of the runs kernel
+#ifdef __CUDACC__
+__shared__ XTab g_runs_xtab[RUNS_WARPS * RUN_R];
+#endif
+UP_HD XTab xtab_entry(const RunCtx &rc, int r, float f) {
+	const float qx = rc.px(r) * f;
+	const float fx0 = floorf(qx);
+	XTab e;
+	e.fx = qx - fx0;
+	e.u = fade(e.fx);
+	e.du = dfade(e.fx);
+	e.cx = (int)fx0;
+	return e;
+}
+
 // per-sample accumulator: value and gradient (Acc4) or value only (float);
 // acc[r * stride] belongs to sample r
 struct alignas(16) Acc4 { float v, gx, gy, gz; };
@@ -105,6 +125,15 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 	const uint32_t y0 = (uint32_t)iy * HY, z0 = ((uint32_t)iz * HZ) ^ key, z1 = ((uint32_t)iz * HZ + HZ) ^ key;
 	const uint32_t yz[4] = {y0 ^ z0, (y0 + HY) ^ z0, y0 ^ z1, (y0 + HY) ^ z1};
 	const float ys[4] = {fy, fy - 1.f, fy, fy - 1.f}, zs[4] = {fz, fz, fz - 1.f, fz - 1.f};
+#ifdef __CUDA_ARCH__
+	XTab *tab = g_runs_xtab + (threadIdx.x >> 5) * RUN_R;
+	__syncwarp(); // every lane has finished reading the previous octave's table
+	if ((int)(threadIdx.x & 31) < R) tab[threadIdx.x & 31] = xtab_entry(rc, (int)(threadIdx.x & 31), f);
+	__syncwarp();
+#else
+	XTab tab[RUN_R];
+	for (int q = 0; q < R; q++) tab[q] = xtab_entry(rc, q, f);
+#endif
 	// coefficients of the two x faces of the current cell; when the next
 	// segment is the neighbouring cell, its low face is the old high face
 	float GX[2], Cc[2], Py[2], Qy[2], Pz[2], Qz[2];
@@ -112,7 +141,7 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 	int r = 0;
 	#pragma unroll 1
 	while (r < R) { // one segment of samples sharing an x cell (the same for every lane)
-		const int cx = (int)floorf(rc.px(r) * f);
+		const int cx = tab[r].cx;
 		const bool carry = r > 0 && cx == cx_prev + 1;
 		cx_prev = cx;
 		if (carry) { GX[0] = GX[1]; Cc[0] = Cc[1]; Py[0] = Py[1]; Qy[0] = Qy[1]; Pz[0] = Pz[1]; Qz[0] = Qz[1]; }
@@ -145,11 +174,10 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 		}
 		#pragma unroll 1
 		for (; r < R; r++) {
-			const float qx = rc.px(r) * f;
-			const float fx0 = floorf(qx);
-			if ((int)fx0 != cx) break;
-			const float fx = qx - fx0;
-			const float u = fade(fx);
+			const XTab e = tab[r];
+			if (e.cx != cx) break;
+			const float fx = e.fx;
+			const float u = e.u;
 			const float A0 = VALUE ? Cc[0] : fx * GX[0] + Cc[0];
 			const float A1 = VALUE ? Cc[1] : (fx - 1.f) * GX[1] + Cc[1];
 			const float dA = A1 - A0;
@@ -157,7 +185,7 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 			float s = n, ds = 1.f;
 			if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
 			if (GRAD) {
-				const float du = dfade(fx);
+				const float du = e.du;
 				const float dnx = (VALUE ? 0.f : GX[0] + u * (GX[1] - GX[0])) + du * dA;
 				const float y0v = VALUE ? Qy[0] : fx * Py[0] + Qy[0], y1v = VALUE ? Qy[1] : (fx - 1.f) * Py[1] + Qy[1];
 				const float z0v = VALUE ? Qz[0] : fx * Pz[0] + Qz[0], z1v = VALUE ? Qz[1] : (fx - 1.f) * Pz[1] + Qz[1];

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 // dynamic shared memory, RUNS_T slots per sample index, so thread t owns
 // acc[r * RUNS_T + t]
 constexpr int RUNS_T = 128;
+static_assert(RUNS_T == 32 * RUNS_WARPS, "the x tables of up_grid_runs.cuh hold one row per warp");
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
 	float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
