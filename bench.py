@@ -311,8 +311,28 @@ def extra_modes(up, stream):
     fn = lambda: planet.sdf_grid(g, 7, outs=outs)  # noqa: E731
     fn()
     ms = _events(stream, fn, 3)
-    return {"ms": ms, "gsamples_s": n / ms / 1e6, "fields": 3,
-            "what": "sphere/lakes/default seed 0, 500^3 over [-2000,2000]^3, land+water+navigation in one pass"}
+    # the land base mesh of the same planet (meshGenerateBaseLand): narrow-band
+    # sampling inside up_contour, and contouring the exactly sampled grid
+    import ctypes as C
+    pos0, _, idx0 = planet.contour(g)
+    V, I = len(pos0), len(idx0)
+    pos = torch.empty((V, 3), device="cuda")
+    nrm = torch.empty((V, 3), device="cuda")
+    idx = torch.empty(I, dtype=torch.int32, device="cuda")
+    mesh = up.abi.MeshOut(pos.data_ptr(), nrm.data_ptr(), idx.data_ptr(), V, I, 0, 0)
+
+    def banded():
+        assert planet.lib.up_contour(planet.h, 0, C.byref(g), None, C.byref(mesh)) == 0
+
+    def full():
+        planet.sdf_grid(g, 1, outs=[outs[0], None, None])
+        assert planet.lib.up_contour(planet.h, 0, C.byref(g), C.c_void_p(outs[0].data_ptr()), C.byref(mesh)) == 0
+    banded()
+    full()
+    return {"ms": ms, "gsamples_s": n / ms / 1e6, "fields": 3, "land_mesh_ms": _events(stream, banded, 3),
+            "land_mesh_full_grid_ms": _events(stream, full, 3), "triangles": I // 3,
+            "what": "sphere/lakes/default seed 0, 500^3 over [-2000,2000]^3: land+water+navigation in one pass (ms); "
+                    "land mesh with narrow-band sampling (land_mesh_ms) and from the exactly sampled grid"}
 
 
 def run_reference(args) -> None:

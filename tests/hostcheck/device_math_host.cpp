@@ -10,6 +10,8 @@
 
 namespace up {
 int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
+void elevation_range(const ModesDesc &D, double &lo, double &hi);
+float modes_contour_band(const ModesDesc &D, int field, const float step[3]);
 }
 
 using namespace up;
@@ -73,6 +75,8 @@ void *hc_modes_create(const char *shape, const char *elevation, const char *colo
 	return D;
 }
 void hc_modes_free(void *d) { delete (ModesDesc *)d; }
+void hc_elevation_range(void *d, double *lo, double *hi) { elevation_range(*(ModesDesc *)d, *lo, *hi); }
+float hc_modes_band(void *d, int field, const float *step) { return modes_contour_band(*(ModesDesc *)d, field, step); }
 void hc_modes_field(void *d, int field, const float *xyz, uint64_t n, float *out, float *grad) {
 	const ModesDesc &M = *(ModesDesc *)d;
 	for (uint64_t i = 0; i < n; i++) {

@@ -133,3 +133,23 @@ def test_synth_noise_bound(H, O):
     # ridged Perlin: |1 - 2|n|| <= 2 * 1.1 - 1 per unit amplitude; cellular F2 - F1 - 1 <= sqrt(6) - 1
     want = 0.04 * 1.2 + 0.02 * (6 ** 0.5 - 1)
     assert abs(H.hc_synth_noise_bound(C.byref(P)) - want) <= 1e-6
+
+
+@pytest.mark.parametrize("elevation", ["none", "simple", "legacy", "lakes", "islands", "craters"])
+def test_elevation_range_holds(H, O, elevation):
+    """The elevation ranges behind the narrow band of reference-mode
+    contouring (elevation_range) contain the oracle's raw elevation."""
+    H.hc_modes_create.restype = C.c_void_p
+    H.hc_modes_create.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_uint32]
+    H.hc_elevation_range.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    H.hc_modes_free.argtypes = [C.c_void_p]
+    for seed in (1, 9):
+        d = H.hc_modes_create(b"sphere", elevation.encode(), b"default", 0, 0, seed)
+        lo, hi = C.c_double(), C.c_double()
+        H.hc_elevation_range(d, C.byref(lo), C.byref(hi))
+        H.hc_modes_free(d)
+        planet = O.Planet("sphere", elevation, "default", seed=seed)
+        x = np.random.default_rng(seed).uniform(-2500, 2500, size=(60000, 3)).astype(np.float32)
+        e = planet.field(4, x)
+        assert lo.value <= e.min() and e.max() <= hi.value, (e.min(), e.max(), lo.value, hi.value)
+        assert hi.value - lo.value <= 20 * max(1.0, e.max() - e.min())  # not vacuous

@@ -103,3 +103,21 @@ def test_mode_contour_matches_oracle(cuda, up, O):
     # the lakes/mountains formulas have gradient kinks (saturate, max, terrace,
     # smoothMax): Hermite normals taken there may come from either side
     assert (err > 1e-3).mean() <= 1e-2 and err.max() <= 1.0
+
+
+@pytest.mark.parametrize("shape,elevation,seed", [("sphere", "lakes", 1), ("torus", "islands", 2), ("cube", "simple", 3),
+                                                 ("box", "legacy", 4), ("h2o", "craters", 5), ("sphere", "none", 6),
+                                                 ("tetrahedron", "lakes", 7), ("knot", "lakes", 8)])
+def test_modes_narrow_band_contour_equals_full_grid(cuda, up, shape, elevation, seed):
+    """Contouring a reference-mode land or navigation field samples the
+    elevation only near the shape's surface (1-Lipschitz shapes; knot takes
+    no band); the meshes equal those of the exactly sampled grid bit for bit."""
+    planet = up.Planet(shape, elevation, "default", seed=seed)
+    g = up.abi.Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), (72, 70, 68))
+    for field in (up.abi.FIELD_LAND, up.abi.FIELD_NAVIGATION):
+        mask = 1 << field
+        full = planet.sdf_grid(g, mask)[field]
+        banded = planet.contour(g, field=field)
+        exact = planet.contour(g, field=field, values=full)
+        for a, b in zip(banded, exact):
+            assert np.array_equal(a, b), (shape, elevation, field)

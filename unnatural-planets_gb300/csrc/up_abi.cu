@@ -19,8 +19,7 @@ namespace up {
 cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, cudaStream_t s);
 int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
 uint32_t instance_seed(uint32_t seed, uint32_t slot);
-cudaError_t launch_modes_grid(const ModesDesc *M, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
-	unsigned *nanflag, cudaStream_t s);
+float modes_contour_band(const ModesDesc &D, int field, const float step[3]);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag,
 	cudaStream_t s);
 cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int purpose, const float *pos, const float *nrm, const float *uv,
@@ -214,7 +213,8 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 		else {
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;
-			check(launch_modes_grid(ctx->d_modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream), "sdf grid kernel");
+			check(launch_modes_grid(ctx->d_modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream,
+				modes_contour_band(ctx->modes, field, c.g.step)), "sdf grid kernel");
 		}
 		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
 		c.d = gd;

@@ -27,9 +27,11 @@ __device__ __forceinline__ void fields_of(const ModesDesc &M, uint32_t mask, V3S
 	out[2] = s - s_max(e, mk<S>(0.f));
 }
 
+// band > 0 (one field, no gradient): samples with |shape| > band take the
+// shape value (narrow band of contouring, modes_contour_band)
 template<bool GRAD>
 __global__ void __launch_bounds__(128) modes_grid_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g, float *__restrict__ o0,
-	float *__restrict__ o1, float *__restrict__ o2, float *__restrict__ grad, unsigned *__restrict__ nanflag) {
+	float *__restrict__ o1, float *__restrict__ o2, float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint64_t plane = (uint64_t)nx * ny * g.n[2];
 	const uint32_t total = (uint32_t)plane;
@@ -48,7 +50,9 @@ __global__ void __launch_bounds__(128) modes_grid_kernel(const ModesDesc *__rest
 			grad[plane + idx] = f[gf].d.y;
 			grad[2 * plane + idx] = f[gf].d.z;
 		} else {
-			fields_of(M, mask, vs(p.x, p.y, p.z), v);
+			const float sh = band > 0.f ? shape_eval(M, vs(p.x, p.y, p.z)) : 0.f;
+			if (band > 0.f && fabsf(sh) > band) v[0] = v[1] = v[2] = sh;
+			else fields_of(M, mask, vs(p.x, p.y, p.z), v);
 		}
 		if (mask & 1u) { o0[idx] = v[0]; bad |= isnan(v[0]); }
 		if (mask & 2u) { o1[idx] = v[1]; bad |= isnan(v[1]); }
@@ -91,10 +95,10 @@ static cudaError_t launch_p(K kernel, uint64_t work, cudaStream_t s, A... args) 
 }
 
 cudaError_t launch_modes_grid(const ModesDesc *M, uint32_t mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag,
-	cudaStream_t s) {
+	cudaStream_t s, float band) {
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
-	if (grad) return launch_p(modes_grid_kernel<true>, n, s, M, mask, g, o0, o1, o2, grad, nanflag);
-	return launch_p(modes_grid_kernel<false>, n, s, M, mask, g, o0, o1, o2, grad, nanflag);
+	if (grad) return launch_p(modes_grid_kernel<true>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, 0.f);
+	return launch_p(modes_grid_kernel<false>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, band);
 }
 
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s) {

@@ -6,6 +6,7 @@
 // coloringModes.cpp (configurations cited per instance below).
 #include "up_modes_desc.h"
 #include "up_noise.cuh"
+#include "up_synth.cuh"
 #include "../../include/up_abi.h"
 
 #include <cmath>
@@ -79,6 +80,75 @@ double unit_draw(uint32_t seed, uint32_t i) { return (mix32(seed ^ (0x85EBCA6BU 
 } // namespace
 
 // returns UP_OK or UP_ERR_INVALID_MODE with err filled
+// |noise_dev(n)| <= this everywhere: the per-type bound (noise_abs_bound)
+// times the sum of |amplitudes|, through 1 - 2|v| for ridged octaves
+static double noise_dev_bound(const NoiseDev &n) {
+	const double nm = noise_abs_bound(n.type, n.dist, n.op);
+	const double sm = n.fractal == UP_FRACTAL_RIDGED ? std::fmax(1.0, 2.0 * nm - 1.0) : nm;
+	double b = 0;
+	for (int i = 0; i < n.octaves; i++) b += std::fabs((double)n.amp[i]) * sm;
+	return b;
+}
+
+// Range [lo, hi] of the elevation of the planet's mode (elevation_eval in
+// up_modes.cuh, elevationModes.cpp), from the noise bounds:
+//  none: 100; simple: 100 - 1000 ((0.3 - n) 1.3 - 0.35)^3 - 100, monotone in n;
+//  legacy: 2500 g(n + 0.11), g(a) = -(-a)^0.85 or a^1.7, monotone;
+//  lakes/islands: land = 150 (x / (|x| + 0.17) + 0.15), |x| <= 1, plus the
+//    mountains, >= 0 and <= max(1000 (r - 0.1)^1.6, 250 (2.5 (t + 0.1) + 1))
+//    + 50 / 4 (smooth max over max; terrace(x) <= x + 1);
+//  craters: 200 + 190 h, h = 10 (x^4 - 0.9 x^5 - 0.1) in [-1, 0.25] for x in [0, 1].
+void elevation_range(const ModesDesc &D, double &lo, double &hi) {
+	switch (D.elevation) {
+		case 0: lo = hi = 100.0; return;
+		case 1: {
+			const double b = noise_dev_bound(D.elev[NS_SIMPLE]);
+			const double t0 = (0.3 - b) * 1.3 - 0.35, t1 = (0.3 + b) * 1.3 - 0.35;
+			lo = 100.0 - (t1 * t1 * t1 + 0.1) * 1000.0;
+			hi = 100.0 - (t0 * t0 * t0 + 0.1) * 1000.0;
+			return;
+		}
+		case 2: {
+			const double b = noise_dev_bound(D.elev[NS_LEGACY_ELEV]);
+			auto g = [](double a) { return a < 0 ? -std::pow(-a, 0.85) : std::pow(a, 1.7); };
+			lo = g(0.11 - b) * 2500.0;
+			hi = g(0.11 + b) * 2500.0;
+			return;
+		}
+		case 3: case 4: {
+			const double x = 1.0 / 1.17;
+			const double ridge = std::pow(std::fmax(noise_dev_bound(D.elev[NS_MTN_RIDGE]) - 0.1, 0.0), 1.6) * 1000.0;
+			const double terr = (std::fmax(noise_dev_bound(D.elev[NS_MTN_TERRACE]) + 0.1, 0.0) * 2.5 + 1.0) * 250.0;
+			lo = (-x + 0.15) * 150.0;
+			hi = (x + 0.15) * 150.0 + std::fmax(ridge, terr) + 12.5;
+			return;
+		}
+		default: lo = 10.0; hi = 200.0 + 0.25 * 190.0; return;
+	}
+}
+
+// Narrow band of contouring a reference-mode field (see contour_band in
+// up_sdf.cu for the argument): the land field is shape - elevation / 10 and
+// navigation shape - max(elevation / 10, 0), so where |shape| exceeds the
+// bound of that term plus the longest grid step, the field has the sign of
+// the shape, and so do its grid neighbours, provided the shape is
+// 1-Lipschitz. That holds for the exact distance functions and their smooth
+// unions, isometries and uniform scalings listed here (sdf.cpp); the other
+// shapes (noise, sine networks, twists, folds, polar repetition, the
+// Mandelbulb estimator) take no band. Returns 0 for no band.
+float modes_contour_band(const ModesDesc &D, int field, const float step[3]) {
+	static const int kLipschitz[] = {2, 3, 5, 6, 7, 8, 11, 12, 13, 15, 17, 22, 24, 25, 26, 27, 28, 30};
+	bool ok = false;
+	for (int s : kLipschitz) ok = ok || D.shape == s;
+	if (!ok || (field != UP_FIELD_LAND && field != UP_FIELD_NAVIGATION)) return 0.f;
+	double lo, hi;
+	elevation_range(D, lo, hi);
+	const double B = field == UP_FIELD_LAND ? std::fmax(std::fabs(lo), std::fabs(hi)) * 0.1 : std::fmax(hi, 0.0) * 0.1;
+	const double st = std::fmax(step[0], std::fmax(step[1], step[2]));
+	const double band = (B + st) * 1.001 + 0.01;
+	return std::isfinite(band) ? (float)band : 0.f;
+}
+
 int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err) {
 	std::memset(&D, 0, sizeof(D));
 	auto S = [&](uint32_t slot) { return instance_seed(seed, slot); };
