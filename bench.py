@@ -17,12 +17,15 @@ After the headline, rank 0 measures the other workloads of the path once
 each ("extras" in the JSON line, each bounded to seconds):
   atlas      4096^2 texel atlas of the 512^3 planet's mesh (raster, synthetic
              coloring program, dilation 7, 8-bit) into device buffers
-  adjoint    sphere - 4-octave simplex FBM: value+gradient forward and the
-             parameter adjoint of L = mean(d^2) on 16,777,216 shell points
+  adjoint    the 512^3 planet's program: value+gradient forward and the
+             adjoint of L = mean(d^2) over its 25 parameters on 16,777,216
+             points of its 0.05 shell
   batch      64 planets x 512 uneven chunks (1.8e8 samples): one batched
              call (graph replay) against one up_contour call per chunk
-  fit        inverse fit, 300 Adam steps (lr 1e-2) on 32M shell points plus
-             a sign loss on the 256^3 grid
+  fit        inverse fit of that program's 25 parameters, 300 Adam steps
+             (lr 1e-2) on 32M shell points plus a sign loss on the 256^3
+             grid; reports |theta - theta*| and the SDF RMS against the
+             FP64 oracle
   modes      reference-mode planet sphere/lakes/default, seed 0, 500^3 over
              [-2000, 2000]^3, land+water+navigation in one pass
   cpu_1t     the CPU baseline on one thread
@@ -182,17 +185,30 @@ def extra_atlas(up, W, planet, stream, pos0, nrm0, idx0):
             "what": "4096^2: raster + synthetic coloring (3-oct value albedo, 2-oct simplex roughness, height) + dilation 7 + U8"}
 
 
-def extra_adjoint(up, W, stream):
+def _shell(planet, n, half_width, seed):
+    """n points uniform in {|d| < half_width} of planet (rejection from the
+    [-1.6, 1.6]^3 box, candidates and their values on the GPU)."""
     import torch
-    P = W.sphere_fbm()
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    got, have = [], 0
+    while have < n:
+        c = (torch.rand((1 << 25, 3), device="cuda", generator=gen) * 3.2 - 1.6).contiguous()
+        d = planet.sdf_points(c, d=torch.empty(c.shape[0], device="cuda"))
+        keep = c[d.abs() < half_width]
+        got.append(keep)
+        have += keep.shape[0]
+    return torch.cat(got)[:n].contiguous()
+
+
+def extra_adjoint(up, W, stream):
+    """the value+adjoint configuration: the torus + 8 spheres - ridged Perlin +
+    cellular planet, 16,777,216 points uniform in its 0.05 shell"""
+    import torch
+    P = W.torus_spheres_ridged_cellular()
     planet = up.Planet(program=P)
     planet.set_stream(stream.cuda_stream)
     n = 1 << 24
-    gen = torch.Generator(device="cuda").manual_seed(11)
-    d = torch.randn((n, 3), device="cuda", generator=gen)
-    d /= d.norm(dim=1, keepdim=True)
-    r = torch.empty(n, device="cuda").uniform_(0.95 ** 3, 1.05 ** 3, generator=gen).pow(1.0 / 3.0)
-    x = (d * r[:, None]).contiguous()
+    x = _shell(planet, n, 0.05, seed=11)
     v = torch.empty(n, device="cuda")
     g = torch.empty((n, 3), device="cuda")
     nt = W.theta_count(P)
@@ -204,7 +220,8 @@ def extra_adjoint(up, W, stream):
     bwd()
     f_ms, b_ms = _events(stream, fwd, 5), _events(stream, bwd, 5)
     return {"points": n, "theta": nt, "forward_ms": f_ms, "backward_ms": b_ms, "backward_gpoints_s": n / b_ms / 1e6,
-            "what": "sphere R=1 - 4-oct simplex FBM; forward value+dd/dp, backward dL/dtheta of mean(d^2), 0.05 shell"}
+            "what": "torus + 8 spheres - ridged perlin + cellular; forward value+dd/dp, backward dL/dtheta of mean(d^2) "
+                    "over the 25 parameters, 16M points uniform in the 0.05 shell"}
 
 
 def extra_batch(up, W, stream):
@@ -253,31 +270,31 @@ def extra_batch(up, W, stream):
 
 
 def extra_fit(up, W, stream, steps=300):
+    """inverse fit of the torus + spheres - ridged Perlin + cellular planet:
+    theta* = the program's 25 parameters scaled by (1 + 0.05 U[-1,1]) from
+    seed 1, theta0 = theta* scaled by (1 + 0.05 U[-1,1]) from seed 2"""
     import numpy as np
     import torch
+    from oracle import oracle as O
     AG = importlib.import_module("unnatural-planets_gb300.autograd")
-    target = W.sphere_fbm(seed=5)
-    t_star = torch.from_numpy(W.theta_of(target)).cuda()
-    gen = torch.Generator(device="cuda").manual_seed(21)
+    P = W.torus_spheres_ridged_cellular()
+    base = W.theta_of(P).astype(np.float64)
+    t_star_np = (base * (1 + 0.05 * np.random.default_rng(1).uniform(-1, 1, size=base.shape))).astype(np.float32)
+    t0 = (t_star_np * (1 + 0.05 * np.random.default_rng(2).uniform(-1, 1, size=base.shape))).astype(np.float32)
+    t_star = torch.from_numpy(t_star_np).cuda()
+    target = up.Planet(program=P)
+    target.set_stream(stream.cuda_stream)
+    target.set_theta(t_star_np)
     n = 32 << 20
-    d = torch.randn((n, 3), device="cuda", generator=gen)
-    d /= d.norm(dim=1, keepdim=True)
-    r = torch.empty(n, device="cuda").uniform_(0.9 ** 3, 1.1 ** 3, generator=gen).pow(1.0 / 3.0)
-    x = (d * r[:, None]).contiguous()
-    gg = W.grid(W.GRID_C1, n=(256, 256, 256))
-    lo = torch.tensor(list(gg.lo), device="cuda")
-    hi = torch.tensor(list(gg.hi), device="cuda")
-    ax = [torch.linspace(float(lo[a]), float(hi[a]), 256, device="cuda") for a in range(3)]
+    x = _shell(target, n, 0.05, seed=21)
+    gg = W.grid(W.GRID_C2, n=(256, 256, 256))
+    ax = [torch.linspace(float(gg.lo[a]), float(gg.hi[a]), 256, device="cuda") for a in range(3)]
     zz, yy, xx = torch.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
     xg = torch.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], dim=1).contiguous()
-    pt = up.Planet(program=target)
-    pt.set_stream(stream.cuda_stream)
-    d_star = pt.sdf_points(x, d=torch.empty(n, device="cuda"))
-    s_star = torch.sign(pt.sdf_points(xg, d=torch.empty(xg.shape[0], device="cuda")))
-    rng = np.random.default_rng(6)
-    t0 = t_star.cpu().numpy() * (1 + 0.15 * rng.uniform(-1, 1, size=t_star.shape[0])).astype(np.float32)
+    d_star = target.sdf_points(x, d=torch.empty(n, device="cuda"))
+    s_star = torch.sign(target.sdf_points(xg, d=torch.empty(xg.shape[0], device="cuda")))
     theta = torch.tensor(t0, device="cuda", requires_grad=True)
-    planet = up.Planet(program=W.sphere_fbm(seed=5))
+    planet = up.Planet(program=W.torus_spheres_ridged_cellular())
     planet.set_stream(stream.cuda_stream)
     opt = torch.optim.Adam([theta], lr=1e-2)
     err0 = float((theta.detach() - t_star).norm() / t_star.norm())
@@ -295,10 +312,17 @@ def extra_fit(up, W, stream, steps=300):
         loss = step()
     torch.cuda.synchronize()
     ms = 1e3 * (time.perf_counter() - t) / (steps - 1)
+    # final SDF against the FP64 oracle at theta* on 65536 of the shell points
+    xs = x[: 1 << 16].cpu().numpy()
+    planet.set_theta(theta.detach().cpu().numpy())
+    fit = planet.sdf_points(xs)
+    ref = O.synth_points(P, xs, theta=t_star_np.astype(np.float64))
     return {"steps": steps, "ms_per_step": ms, "points": n, "sign_points": int(xg.shape[0]), "loss": float(loss.detach()),
             "theta_rel_err_start": err0, "theta_rel_err_end": float((theta.detach() - t_star).norm() / t_star.norm()),
-            "what": "sphere - 4-oct simplex FBM, theta* seed 5, theta0 = theta* (1 + 0.15 U[-1,1]) seed 6; "
-                    "L = mean((d - d*)^2) on 32M shell points + mean(relu(-d sign(d*))) on 256^3"}
+            "sdf_rms_vs_fp64_oracle": float(np.sqrt(np.mean((fit - ref) ** 2))),
+            "what": "torus + 8 spheres - ridged perlin + cellular, 25 parameters; theta* = theta (1 + 0.05 U) seed 1, "
+                    "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell + "
+                    "mean(relu(-d sign(d*))) on 256^3; Adam lr 1e-2; SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
 
 
 def extra_modes(up, stream):
