@@ -254,7 +254,7 @@ void contour_geometry(up_context *ctx, int field, ContourRun &c, float *pos, flo
 // slab k + 1. Slab coordinates use the full grid's index (GridDev::k0), so
 // values are bit-identical to the single launch.
 constexpr size_t GRID_PIPE_MIN = (size_t)1 << 22; // samples
-constexpr int GRID_PIPE_SLABS = 8;
+constexpr int GRID_PIPE_SLABS = 16;
 int sdf_grid_pipelined(up_context *ctx, uint32_t mask, const GridDev &g, float *const out[3], float *grad) {
 	if (!ctx->copy_stream) {
 		check(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
