@@ -215,7 +215,10 @@ float up_sdf_navigation(const float p[3]);
  * LAND/WATER/NAVIGATION written in ONE pass (shape and elevation evaluated
  * once per sample); out[f] receives nx*ny*nz floats for each selected field f
  * (index by up_field). grad, when not NULL, receives 3*nx*ny*nz floats
- * (planes gx, gy, gz) of the analytic gradient of the lowest selected field. */
+ * (planes gx, gy, gz) of the analytic gradient of the lowest selected field.
+ * Outputs may be host or device memory; when all are host memory the grid is
+ * sampled in z-slabs whose device-to-host copies overlap the sampling of the
+ * next slab. Values are exact everywhere (no narrow band). */
 int up_sdf_grid(up_context *ctx, uint32_t fields_mask, const up_grid *grid, float *const out[3], float *grad);
 
 /* ---------------------------------------------------------------- contour */
@@ -328,7 +331,9 @@ typedef struct up_batch_out {
  * pass per stage, each stage one launch over all chunks, replayed as a CUDA
  * graph when the same chunk list is run again. The closest reference
  * counterpart is the per-chunk tasksRunBlocking fan-out (generator.cpp:159,215).
- * Indices of chunk c are local to chunk c's vertices. */
+ * Indices of chunk c are local to chunk c's vertices. Without a values buffer
+ * the chunks are sampled with the narrow band of contouring (see up_contour;
+ * the meshes are the same); with one, every sample is exact. */
 int up_batch_run(up_context *ctx, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks, up_batch_out *out);
 
 #ifdef __cplusplus
