@@ -310,50 +310,69 @@ UP_HD V3f cell_dist_grad(V3f v, float F, int dist) {
 }
 
 // DIST/OP >= 0 fix the metric/output at compile time; -1 reads them at run time.
-// Euclidean candidates are compared by squared length (sqrt is monotone and
-// correctly rounded, so F1/F2 are the same as comparing the lengths).
+// Candidates are ranked by an integer key: the distance (squared length for
+// Euclidean; every metric is >= 0, so float bits order like values) with its
+// low 6 mantissa bits replaced by the candidate id (dz, dy, dx order, the
+// search order). The two smallest keys take three integer min/max per
+// candidate; the winners' exact distances and difference vectors are then
+// rebuilt from their ids. Exact ties keep the first candidate in search
+// order; distances within 2^-17 relative of each other may be ranked by id.
+template<int DIST>
+UP_HD float cell_dist(float vx, float vy, float vz, int dist) {
+	const int m = DIST >= 0 ? DIST : dist;
+	const float e2 = vx * vx + vy * vy + vz * vz;
+	if (m == 0) return e2;
+	const float m1 = fabsf(vx) + fabsf(vy) + fabsf(vz);
+	if (m == 1) return m1;
+	return e2 + m1;
+}
 template<bool GRAD, int DIST = -1, int OP = -1>
 UP_HD NG cellular_n(V3f p, uint32_t key, int dist_rt, int op_rt) {
 	const int dist = DIST >= 0 ? DIST : dist_rt;
 	const int op = OP >= 0 ? OP : op_rt;
 	const Cell c = cell_of(p);
-	float F1 = 1e20f, F2 = 1e20f;
-	V3f g1 = zero3(), g2 = zero3();
-	uint32_t cellh = 0;
+	uint32_t K1 = 0xFFFFFFFFu, K2 = 0xFFFFFFFFu;
 	#pragma unroll 1
 	for (int dz = -1; dz <= 1; dz++) {
 		const uint32_t zh = ((uint32_t)(c.iz + dz) * HZ) ^ key;
 		#pragma unroll 1
 		for (int dy = -1; dy <= 1; dy++) {
 			const uint32_t yzh = ((uint32_t)(c.iy + dy) * HY) ^ zh;
+			const uint32_t id0 = (uint32_t)((dz + 1) * 9 + (dy + 1) * 3);
 			#pragma unroll
 			for (int dx = -1; dx <= 1; dx++) {
 				const uint32_t h = mix32(((uint32_t)(c.ix + dx) * HX) ^ yzh);
 				const float vx = ((float)dx + jitter(h, 0)) - c.fx;
 				const float vy = ((float)dy + jitter(h, 10)) - c.fy;
 				const float vz = ((float)dz + jitter(h, 20)) - c.fz;
-				float d;
-				const float e2 = vx * vx + vy * vy + vz * vz;
-				if (dist == 0) d = e2;
-				else if (dist == 1) d = fabsf(vx) + fabsf(vy) + fabsf(vz);
-				else d = e2 + (fabsf(vx) + fabsf(vy) + fabsf(vz));
-				if (d < F1) {
-					F2 = F1; F1 = d;
-					if (OP == 0 || (OP < 0 && op == 0)) cellh = h;
-					if (GRAD) { g2 = g1; g1 = v3(vx, vy, vz); }
-				} else if (d < F2) {
-					F2 = d;
-					if (GRAD) g2 = v3(vx, vy, vz);
-				}
+				const uint32_t k = (f_bits(cell_dist<DIST>(vx, vy, vz, dist)) & ~63u) | (id0 + (uint32_t)(dx + 1));
+				K2 = K2 < (K1 > k ? K1 : k) ? K2 : (K1 > k ? K1 : k);
+				K1 = K1 < k ? K1 : k;
 			}
 		}
 	}
+	float F[2];
+	V3f g[2];
+	uint32_t cellh = 0;
+	#pragma unroll
+	for (int w = 0; w < 2; w++) {
+		const uint32_t id = (w ? K2 : K1) & 63u;
+		const int dz = (int)(id / 9u) - 1, dy = (int)((id / 3u) % 3u) - 1, dx = (int)(id % 3u) - 1;
+		const uint32_t h = mix32(((uint32_t)(c.ix + dx) * HX) ^ ((uint32_t)(c.iy + dy) * HY) ^ (((uint32_t)(c.iz + dz) * HZ) ^ key));
+		const float vx = ((float)dx + jitter(h, 0)) - c.fx;
+		const float vy = ((float)dy + jitter(h, 10)) - c.fy;
+		const float vz = ((float)dz + jitter(h, 20)) - c.fz;
+		F[w] = cell_dist<DIST>(vx, vy, vz, dist);
+		g[w] = v3(vx, vy, vz);
+		if (w == 0) cellh = h;
+	}
+	float F1 = F[0], F2 = F[1];
 	if (dist == 0) { F1 = sqrtf(F1); F2 = sqrtf(F2); }
 	// d F / d p for the stored difference vectors v = q - p (dv/dp = -I)
 	V3f dF1 = zero3(), dF2 = zero3();
 	if (GRAD) {
-		dF1 = cell_dist_grad(g1, F1, dist);
-		dF2 = cell_dist_grad(g2, F2, dist);
+		dF1 = cell_dist_grad(g[0], F1, dist);
+		dF2 = cell_dist_grad(g[1], F2, dist);
 	}
 	switch (op) {
 		case 0: return ngc(hash_signed(mix32(cellh)));
