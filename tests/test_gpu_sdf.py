@@ -150,3 +150,26 @@ def test_host_outputs_pipelined_equal_device(cuda, up):
     host = mp.sdf_grid(gm, 7)
     for a, b in zip(host, dev):
         assert np.array_equal(a, b.cpu().numpy())
+
+
+@pytest.mark.parametrize("n", [(2, 2, 2), (3, 5, 7), (17, 2, 9), (2, 33, 3)])
+def test_tiny_and_ragged_grids(cuda, up, O, n):
+    """Grids smaller than one warp task (16 x-samples of 8 x 4 rows) and
+    ragged in every axis: values and gradients against the oracle, and
+    contouring either succeeds or reports an empty mesh."""
+    W = workloads()
+    for P in (W.torus_spheres_ridged_cellular(), W.sphere_fbm()):
+        g = up.abi.Grid.make((-1.2, -0.9, -1.1), (1.3, 1.0, 0.7), n)
+        planet = up.Planet(program=P)
+        cnt = g.count
+        d = np.empty(cnt, np.float32)
+        gr = np.empty(3 * cnt, np.float32)
+        planet.sdf_grid(g, 1, outs=[d, None, None], grad=gr)
+        ref, rg = O.synth_points(P, O.grid_positions(g), grad=True)
+        assert np.abs(d - ref).max() <= 1e-5
+        assert np.abs(gr.reshape(3, cnt).T - rg).max() <= 1e-3 * max(1.0, float(np.abs(rg).max()))
+        try:
+            pos, _, idx = planet.contour(g)
+            assert len(idx) % 6 == 0 and (idx < len(pos)).all()
+        except up.UpError as e:
+            assert e.status == up.abi.UP_ERR_EMPTY_MESH
