@@ -213,6 +213,26 @@ UP_HD float cell_metric(float vx, float e2yz, float m1yz) {
 	if (DIST == 1) return fabsf(vx) + m1yz;
 	return (vx * vx + e2yz) + (fabsf(vx) + m1yz);
 }
+// Candidate cells of a warp's cellular sub-run, shared: when the lanes' y and
+// z cells span at most two values each, the union of their 3x3 neighbourhoods
+// times the sub-run's columns fits a 4 x 4 x 4 table that the lanes hash
+// together (two cells each) and every lane reads (broadcasts); otherwise each
+// lane hashes its own candidates. Entry (col, yy, zz) at (col * 4 + yy) * 4 + zz
+// holds the cell's jitter and hash.
+struct CellEntry { float jx, jy, jz; uint32_t h; };
+constexpr int CT = 4;
+#ifdef __CUDACC__
+__shared__ CellEntry g_runs_cells[RUNS_WARPS * CT * CT * CT];
+#endif
+UP_HD CellEntry cell_entry(uint32_t h) {
+	CellEntry c;
+	c.jx = jitter(h, 0);
+	c.jy = jitter(h, 10);
+	c.jz = jitter(h, 20);
+	c.h = h;
+	return c;
+}
+
 template<bool GRAD, int DIST, int OP>
 UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
 	constexpr int S = CELL_SUB;
@@ -239,9 +259,33 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 	#pragma unroll
 	for (int r = 0; r < S; r++) { K1[r] = 0xFFFFFFFFu; K2[r] = 0xFFFFFFFFu; }
 	const int ncol = ixb - ixa + 3;
+	int ty = 0, tz = 0; // this lane's offsets into the shared table
+	bool table = false;
+#ifdef __CUDA_ARCH__
+	const int iymin = __reduce_min_sync(0xFFFFFFFFu, iy), iymax = __reduce_max_sync(0xFFFFFFFFu, iy);
+	const int izmin = __reduce_min_sync(0xFFFFFFFFu, iz), izmax = __reduce_max_sync(0xFFFFFFFFu, iz);
+	table = iymax - iymin <= 1 && izmax - izmin <= 1; // the same for every lane
+	CellEntry *ct = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
+	if (table) {
+		__syncwarp(); // the previous sub-run's readers are done
+		for (int e = (int)(threadIdx.x & 31); e < ncol * CT * CT; e += 32) {
+			const int col = e / (CT * CT), yy = (e / CT) % CT, zz = e % CT;
+			ct[e] = cell_entry(mix32(((uint32_t)(ixa - 1 + col) * HX) ^ ((uint32_t)(iymin - 1 + yy) * HY) ^ (((uint32_t)(izmin - 1 + zz) * HZ) ^ key)));
+		}
+		__syncwarp();
+		ty = iy - iymin + 1;
+		tz = iz - izmin + 1;
+	}
+#endif
+	// candidate cell (column col, neighbour dy, dz) of this lane
+	auto cand = [&](int col, int dy, int dz) -> CellEntry {
+#ifdef __CUDA_ARCH__
+		if (table) return ct[(col * CT + ty + dy) * CT + tz + dz];
+#endif
+		return cell_entry(mix32(((uint32_t)(ixa - 1 + col) * HX) ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key)));
+	};
 	#pragma unroll 1
 	for (int col = 0; col < ncol; col++) {
-		const uint32_t xh = (uint32_t)(ixa - 1 + col) * HX;
 		// a column outside a sample's 3x3x3 neighbourhood is pushed far away
 		float sc[S];
 		#pragma unroll
@@ -250,10 +294,10 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		#pragma unroll 1
 		for (int yz = 0; yz < 9; yz++) {
 			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
-			const uint32_t h = mix32(xh ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
-			const float vy = ((float)dy + jitter(h, 10)) - fy;
-			const float vz = ((float)dz + jitter(h, 20)) - fz;
-			const float T = fcol + jitter(h, 0);
+			const CellEntry ce = cand(col, dy, dz);
+			const float vy = ((float)dy + ce.jy) - fy;
+			const float vz = ((float)dz + ce.jz) - fz;
+			const float T = fcol + ce.jx;
 			const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
 			const uint32_t id = (uint32_t)(col * 9 + yz);
 			#pragma unroll
@@ -274,10 +318,10 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 			const uint32_t id = (wsel ? K2[r] : K1[r]) & 63u;
 			const int col = (int)(id / 9u), yz = (int)(id % 9u);
 			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
-			const uint32_t h = mix32(((uint32_t)(ixa - 1 + col) * HX) ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key));
-			const float vy = ((float)dy + jitter(h, 10)) - fy;
-			const float vz = ((float)dz + jitter(h, 20)) - fz;
-			const float vx = ((float)(col - 1) + jitter(h, 0)) - sx[r];
+			const CellEntry ce = cand(col, dy, dz);
+			const float vy = ((float)dy + ce.jy) - fy;
+			const float vz = ((float)dz + ce.jz) - fz;
+			const float vx = ((float)(col - 1) + ce.jx) - sx[r];
 			const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
 			Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
 			vw[wsel] = v3(vx, vy, vz);
@@ -286,7 +330,7 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 				if (DIST == 0) dFw[wsel] = d > 0.f ? vw[wsel] * -rsqrt_hd(d) : zero3();
 				else dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
 			}
-			if (!wsel) h1 = h;
+			if (!wsel) h1 = ce.h;
 		}
 		const float a = Fw[0], b = Fw[1];
 		const V3f dF1 = dFw[0], dF2 = dFw[1];
