@@ -74,3 +74,47 @@ def test_texture_planet(cuda, up, O, purpose):
     for k in ("albedo", "special", "height"):
         diff = np.abs(got[k].astype(int) - want[k].astype(int))
         assert (diff > 2).mean() <= 5e-3, (k, (diff > 2).mean())
+
+
+def _dilate_f32(img, rounds):
+    """tex_dilate_kernel restated in numpy float32: a NaN texel with valid
+    8-neighbours becomes their mean, neighbours summed in (dy, dx) order."""
+    img = img.astype(np.float32).copy()
+    H, W, _ = img.shape
+    for _ in range(rounds):
+        valid = ~np.isnan(img[..., 0])
+        acc = np.zeros_like(img)
+        cnt = np.zeros((H, W), np.int32)
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                if dx == 0 and dy == 0:
+                    continue
+                nb = np.full_like(img, np.nan)
+                ys, yd = (slice(max(dy, 0), H + min(dy, 0)), slice(max(-dy, 0), H + min(-dy, 0)))
+                xs, xd = (slice(max(dx, 0), W + min(dx, 0)), slice(max(-dx, 0), W + min(-dx, 0)))
+                nb[yd, xd] = img[ys, xs]
+                m = ~np.isnan(nb[..., 0])
+                acc[m] = acc[m] + nb[m]
+                cnt += m
+        fill = ~valid & (cnt > 0)
+        out = img.copy()
+        ic = np.float32(1) / cnt[fill].astype(np.float32)
+        out[fill] = acc[fill] * ic[:, None]
+        img = out
+    return img
+
+
+@pytest.mark.parametrize("rounds", [7, 3])
+def test_dilation_bit_exact(cuda, up, O, rounds):
+    """The fused dilation (all rounds in shared-memory tiles) equals the
+    round-by-round rule applied to the undilated float images, bit for bit."""
+    W = workloads()
+    P, (p2, n2, uv, i2) = _mesh(up, O, W)
+    planet = up.Planet(program=P)
+    raw = planet.texture(1, p2, n2, uv, i2, 384, 320, dilation=0, floats=True)
+    got = planet.texture(1, p2, n2, uv, i2, 384, 320, dilation=rounds, floats=True)
+    stack = lambda r: np.concatenate([r["albedo_f"], r["special_f"], r["height_f"][..., None]], axis=2)  # noqa: E731
+    want = _dilate_f32(stack(raw), rounds)
+    have = stack(got)
+    assert np.array_equal(np.isnan(want), np.isnan(have))
+    assert np.array_equal(np.nan_to_num(want, nan=0.0), np.nan_to_num(have, nan=0.0))

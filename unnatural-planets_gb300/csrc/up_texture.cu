@@ -87,23 +87,28 @@ __global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_
 		long long e[3];
 		const uint32_t x = (uint32_t)(q % W), y = (uint32_t)(q / W);
 		tri_cover(f, (long long)x * 256 + 128, (long long)y * 256 + 128, e);
+		// barycentric weights from the exact edge functions: FP64 for the
+		// position (one reciprocal of the area), FP32 for the normal (its
+		// direction does not depend on the area)
+		const double ia = 1.0 / (double)f.area;
 		double w[3];
-		w[f.o[0]] = (double)e[0] / (double)f.area;
-		w[f.o[1]] = (double)e[1] / (double)f.area;
-		w[f.o[2]] = (double)e[2] / (double)f.area;
-		double p[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
+		float wf[3];
+		#pragma unroll
+		for (int k = 0; k < 3; k++) {
+			w[f.o[k]] = (double)e[k] * ia;
+			wf[f.o[k]] = (float)e[k];
+		}
+		double p[3] = {0, 0, 0};
+		V3f nsum = zero3();
 		#pragma unroll
 		for (int k = 0; k < 3; k++) {
 			const uint64_t v = m.idx[3 * (uint64_t)t + k];
 			#pragma unroll
-			for (int a = 0; a < 3; a++) {
-				p[a] += (double)m.pos[3 * v + a] * w[k];
-				nn[a] += (double)m.nrm[3 * v + a] * w[k];
-			}
+			for (int a = 0; a < 3; a++) p[a] += (double)m.pos[3 * v + a] * w[k];
+			if (!SYNTH) nsum = nsum + v3(m.nrm[3 * v], m.nrm[3 * v + 1], m.nrm[3 * v + 2]) * wf[k];
 		}
-		const double ln = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
 		const V3f pf = v3((float)p[0], (float)p[1], (float)p[2]);
-		const V3f nf = v3((float)(nn[0] / ln), (float)(nn[1] / ln), (float)(nn[2] / ln));
+		const V3f nf = SYNTH ? zero3() : nsum * (1.f / sqrtf(dot(nsum, nsum)));
 		V3f albedo;
 		float rough, metal = 0.f, height, opacity = 1.f;
 		if (SYNTH) {
@@ -149,6 +154,78 @@ __global__ void __launch_bounds__(256) tex_dilate_kernel(const float *__restrict
 }
 
 __device__ __forceinline__ uint8_t to_u8(float v) { return isnan(v) ? (uint8_t)0 : (uint8_t)(fminf(fmaxf(v, 0.f), 1.f) * 255.f + 0.5f); }
+
+// All dilation rounds and the output split in one kernel: a block loads a
+// DT_X x DT_Y tile with a halo of `rounds` texels into shared memory, runs
+// the rounds there and writes the tile's final texels to the caller's images.
+// One buffer is updated in place: tag[i] is the round after which texel i is
+// valid (0 = covered, DT_ABSENT = outside the image, DT_NAN = not yet), and
+// round k fills a NaN texel from the neighbours with tag < k (the texels
+// valid before round k, exactly those tex_dilate_kernel reads), so texels
+// filled in round k are not read in round k. Round k updates the region k
+// texels in from the loaded edge. Same arithmetic and neighbour order as
+// tex_dilate_kernel.
+constexpr int DT_X = 32, DT_Y = 16, DT_MAX_ROUNDS = 16;
+constexpr uint8_t DT_ABSENT = 254, DT_NAN = 255;
+__host__ __device__ inline size_t dilate_smem(int rounds, int nch) {
+	const size_t t = (size_t)(DT_X + 2 * rounds) * (DT_Y + 2 * rounds);
+	return sizeof(float) * t * nch + ((t + 15) & ~(size_t)15);
+}
+__global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__restrict__ img, uint32_t W, uint32_t H, int nch, int ach, int rounds,
+	uint8_t *__restrict__ a8, uint8_t *__restrict__ s8, uint8_t *__restrict__ h8, float *__restrict__ af, float *__restrict__ sf,
+	float *__restrict__ hf) {
+	extern __shared__ float dsm[];
+	const int SX = DT_X + 2 * rounds, SY = DT_Y + 2 * rounds;
+	float *A = dsm;
+	uint8_t *tag = (uint8_t *)(dsm + (size_t)SX * SY * nch);
+	const int x0 = (int)(blockIdx.x * DT_X) - rounds, y0 = (int)(blockIdx.y * DT_Y) - rounds;
+	for (int i = threadIdx.x; i < SX * SY; i += blockDim.x) {
+		const int gx = x0 + i % SX, gy = y0 + i / SX;
+		const bool in = gx >= 0 && gy >= 0 && gx < (int)W && gy < (int)H;
+		const float *src = img + ((uint64_t)(in ? gy : 0) * W + (in ? gx : 0)) * nch;
+		for (int c = 0; c < nch; c++) A[i * nch + c] = in ? src[c] : NAN;
+		tag[i] = !in ? DT_ABSENT : (isnan(src[0]) ? DT_NAN : 0);
+	}
+	__syncthreads();
+	for (int k = 1; k <= rounds; k++) {
+		const int rx = SX - 2 * k, ry = SY - 2 * k;
+		for (int j = threadIdx.x; j < rx * ry; j += blockDim.x) {
+			const int lx = k + j % rx, ly = k + j / rx;
+			const int i = ly * SX + lx;
+			if (tag[i] != DT_NAN) continue;
+			float acc[7] = {0, 0, 0, 0, 0, 0, 0};
+			int cnt = 0;
+			for (int dy = -1; dy <= 1; dy++)
+				for (int dx = -1; dx <= 1; dx++) {
+					if (!dx && !dy) continue;
+					const int ni = (ly + dy) * SX + lx + dx;
+					if (tag[ni] >= k) continue; // not valid before this round (or absent)
+					const float *r = A + ni * nch;
+					for (int c = 0; c < nch; c++) acc[c] += r[c];
+					cnt++;
+				}
+			if (!cnt) continue;
+			const float ic = 1.f / (float)cnt;
+			for (int c = 0; c < nch; c++) A[i * nch + c] = acc[c] * ic;
+			tag[i] = (uint8_t)k;
+		}
+		__syncthreads();
+	}
+	for (int j = threadIdx.x; j < DT_X * DT_Y; j += blockDim.x) {
+		const int gx = (int)(blockIdx.x * DT_X) + j % DT_X, gy = (int)(blockIdx.y * DT_Y) + j / DT_X;
+		if (gx >= (int)W || gy >= (int)H) continue;
+		const float *v = A + ((rounds + j / DT_X) * SX + rounds + j % DT_X) * nch;
+		const uint64_t q = (uint64_t)gy * W + gx;
+		for (int c = 0; c < ach; c++) {
+			if (a8) a8[q * ach + c] = to_u8(v[c]);
+			if (af) af[q * ach + c] = v[c];
+		}
+		if (s8) { s8[2 * q] = to_u8(v[ach]); s8[2 * q + 1] = to_u8(v[ach + 1]); }
+		if (sf) { sf[2 * q] = v[ach]; sf[2 * q + 1] = v[ach + 1]; }
+		if (h8) h8[q] = to_u8(v[ach + 2]);
+		if (hf) hf[q] = v[ach + 2];
+	}
+}
 
 // split the interleaved working image into the caller's images
 __global__ void __launch_bounds__(256) tex_output_kernel(const float *__restrict__ img, uint64_t n, int ach, uint8_t *__restrict__ a8,
@@ -213,14 +290,24 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
 	}
 	L++;
-	float *cur = img0, *nxt = img1;
-	for (int r = 0; r < dilation; r++) {
-		tex_dilate_kernel<<<blocks_for((const void *)tex_dilate_kernel, 256, n), 256, 0, s>>>(cur, nxt, W, H, nch);
+	if (dilation > 0 && dilation <= DT_MAX_ROUNDS) {
+		// every round and the output split in one launch (shared-memory tiles)
+		const size_t smem = dilate_smem(dilation, nch);
+		e = cudaFuncSetAttribute((const void *)tex_dilate_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		const dim3 grid((W + DT_X - 1) / DT_X, (H + DT_Y - 1) / DT_Y);
+		tex_dilate_fused_kernel<<<grid, 256, smem, s>>>(img0, W, H, nch, ach, dilation, a8, s8, h8, af, sf, hf);
 		L++;
-		float *t = cur; cur = nxt; nxt = t;
+	} else {
+		float *cur = img0, *nxt = img1;
+		for (int r = 0; r < dilation; r++) {
+			tex_dilate_kernel<<<blocks_for((const void *)tex_dilate_kernel, 256, n), 256, 0, s>>>(cur, nxt, W, H, nch);
+			L++;
+			float *t = cur; cur = nxt; nxt = t;
+		}
+		tex_output_kernel<<<blocks_for((const void *)tex_output_kernel, 256, n), 256, 0, s>>>(cur, n, ach, a8, s8, h8, af, sf, hf);
+		L++;
 	}
-	tex_output_kernel<<<blocks_for((const void *)tex_output_kernel, 256, n), 256, 0, s>>>(cur, n, ach, a8, s8, h8, af, sf, hf);
-	L++;
 	if (launches) *launches = L;
 	return cudaGetLastError();
 }
