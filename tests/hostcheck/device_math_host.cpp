@@ -5,6 +5,7 @@
 #include "../../unnatural-planets_gb300/csrc/up_synth.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_grid_runs.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_modes.cuh"
+#include "../../unnatural-planets_gb300/csrc/up_modes_runs.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_coloring.cuh"
 #include <string>
 
@@ -146,4 +147,54 @@ void hc_grid_runs(const up_synth_program *P, const float *lo, const float *step,
 				}
 			}
 }
+
+// land, water, navigation over a grid through the run tables of
+// up_modes_runs.cuh (the x-coherent modes kernel's arithmetic, one run at a
+// time); returns 0 when the mode has no run tables
+int hc_modes_grid_runs(void *d, const float *lo, const float *step, const uint32_t *n, float band, float *o0, float *o1, float *o2) {
+	const ModesDesc &M = *(ModesDesc *)d;
+	if (!mrun_applies(M)) return 0;
+	constexpr int R = RUN_R;
+	auto coord = [&](int a, uint32_t i) { volatile float m = (float)i * step[a]; return m + lo[a]; };
+	RunCtx rc;
+	rc.lo_x = lo[0];
+	rc.step_x = step[0];
+	rc.nx = n[0];
+	float tab[3 * R], *outs[3] = {o0, o1, o2};
+	for (uint32_t k = 0; k < n[2]; k++)
+		for (uint32_t j = 0; j < n[1]; j++)
+			for (uint32_t i0 = 0; i0 < n[0]; i0 += R) {
+				rc.i0 = i0;
+				rc.py = coord(1, j);
+				rc.pz = coord(2, k);
+				if (M.elevation == 2) modes_run_fill<2>(M, rc, R, tab, 1);
+				else if (M.elevation == 3) modes_run_fill<3>(M, rc, R, tab, 1);
+				else modes_run_fill<4>(M, rc, R, tab, 1);
+				for (int r = 0; r < R && i0 + r < n[0]; r++) {
+					const float sh = shape_eval(M, vs(rc.px(r), rc.py, rc.pz));
+					float v[3];
+					if (M.elevation == 2) modes_run_fields<2>(M, rc, r, sh, true, band, tab, 1, v);
+					else if (M.elevation == 3) modes_run_fields<3>(M, rc, r, sh, true, band, tab, 1, v);
+					else modes_run_fields<4>(M, rc, r, sh, true, band, tab, 1, v);
+					const uint64_t idx = ((uint64_t)k * n[1] + j) * n[0] + i0 + r;
+					for (int f = 0; f < 3; f++) outs[f][idx] = v[f];
+				}
+			}
+	return 1;
 }
+
+// synth_base at R samples of the segment x in [x0, x1] at (y, z): with the
+// sphere mask of synth_segment_spheres (v, g into out_m) and testing every
+// sphere (out_f); returns the mask
+uint32_t hc_segment_base(const up_synth_program *P, float x0, float x1, float y, float z, int R, float *out_m, float *out_f) {
+	const uint32_t live = synth_segment_spheres(*P, x0, x1, y, z);
+	for (int r = 0; r < R; r++) {
+		const float x = R > 1 ? x0 + (x1 - x0) * (float)r / (float)(R - 1) : x0;
+		const NG a = synth_base<true>(*P, v3(fminf(x, x1), y, z), live), b = synth_base<true>(*P, v3(fminf(x, x1), y, z));
+		out_m[4 * r] = a.v; out_m[4 * r + 1] = a.g.x; out_m[4 * r + 2] = a.g.y; out_m[4 * r + 3] = a.g.z;
+		out_f[4 * r] = b.v; out_f[4 * r + 1] = b.g.x; out_f[4 * r + 2] = b.g.y; out_f[4 * r + 3] = b.g.z;
+	}
+	return live;
+}
+}
+

@@ -153,3 +153,64 @@ def test_elevation_range_holds(H, O, elevation):
         e = planet.field(4, x)
         assert lo.value <= e.min() and e.max() <= hi.value, (e.min(), e.max(), lo.value, hi.value)
         assert hi.value - lo.value <= 20 * max(1.0, e.max() - e.min())  # not vacuous
+
+
+@pytest.mark.parametrize("elevation,shape", [("lakes", "sphere"), ("islands", "torus"), ("legacy", "box")])
+def test_modes_grid_runs_equal_per_sample(H, O, elevation, shape):
+    """The x-coherent reference-mode grid path (run tables of the lattice
+    instances, up_modes_runs.cuh) against the per-sample fields and the FP32
+    oracle, with a ragged run tail (45 is not a multiple of the run length)."""
+    H.hc_modes_create.restype = C.c_void_p
+    H.hc_modes_create.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_uint32]
+    H.hc_modes_free.argtypes = [C.c_void_p]
+    H.hc_modes_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
+    H.hc_modes_grid_runs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    d = H.hc_modes_create(shape.encode(), elevation.encode(), b"default", 0, 0, 4)
+    n = (45, 30, 28)
+    g = _abi().Grid.make((-2000, -1900, -1800), (2000, 1900, 1800), n)
+    lo = np.array(g.lo[:], np.float32)
+    st = np.array([(g.hi[a] - g.lo[a]) / np.float32(g.n[a] - 1) for a in range(3)], np.float32)
+    nn = np.array(n, np.uint32)
+    N = g.count
+    outs = [np.empty(N, np.float32) for _ in range(3)]
+    assert H.hc_modes_grid_runs(d, lo.ctypes.data, st.ctypes.data, nn.ctypes.data, 0.0, *[o.ctypes.data for o in outs]) == 1
+    pos = O.grid_positions(g)
+    planet = O.Planet(shape, elevation, "default", seed=4)
+    for f in range(3):
+        ps = np.empty(N, np.float32)
+        H.hc_modes_field(d, f, pos.ctypes.data, N, ps.ctypes.data, None)
+        rel = np.abs(outs[f].astype(np.float64) - ps) / np.maximum(1.0, np.abs(ps))
+        assert (rel > 1e-5).mean() <= 1e-3, (f, rel.max())
+        ref = planet.field(f, pos, precision=1)
+        assert (np.abs(outs[f].astype(np.float64) - ref) / np.maximum(1.0, np.abs(ref)) > 1e-4).mean() <= 5e-3
+    H.hc_modes_free(d)
+
+
+def test_segment_sphere_culling_is_exact(H):
+    """synth_segment_spheres: a sphere left out of a run's mask would be
+    skipped by synth_base's own test at every sample, so the union (value and
+    gradient) is bit-identical with and without the mask; the mask does drop
+    spheres (the runs kernel's saving is real)."""
+    W = workloads()
+    H.hc_segment_base.restype = C.c_uint32
+    H.hc_segment_base.argtypes = [C.POINTER(_abi().SynthProgram), C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p, C.c_void_p]
+    P = W.torus_spheres_ridged_cellular()
+    r = np.random.default_rng(5)
+    R = 16
+    dropped = 0
+    for t in range(4000):
+        if t % 2:  # segments through or next to a sphere
+            s = int(r.integers(P.n_spheres))
+            c = np.array(P.sphere[s][:3]) + r.normal(0, P.sphere[s][3] + P.k, 3)
+        else:
+            c = r.uniform(-1.6, 1.6, 3)
+        ln = float(r.uniform(0.0, 0.2))
+        x0, y, z = np.float32(c[0] - ln / 2), np.float32(c[1]), np.float32(c[2])
+        x1 = np.float32(x0 + ln)
+        om = np.empty(4 * R, np.float32)
+        of = np.empty(4 * R, np.float32)
+        live = H.hc_segment_base(C.byref(P), x0, x1, y, z, R, om.ctypes.data, of.ctypes.data)
+        assert np.array_equal(om, of), (x0, x1, y, z, live)
+        dropped += P.n_spheres - bin(live & ((1 << P.n_spheres) - 1)).count("1")
+    assert dropped > 4000 * P.n_spheres // 2
+

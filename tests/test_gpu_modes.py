@@ -121,3 +121,22 @@ def test_modes_narrow_band_contour_equals_full_grid(cuda, up, shape, elevation, 
         exact = planet.contour(g, field=field, values=full)
         for a, b in zip(banded, exact):
             assert np.array_equal(a, b), (shape, elevation, field)
+
+
+@pytest.mark.parametrize("shape,elevation,seed", [("sphere", "lakes", 3), ("torus", "islands", 5), ("box", "legacy", 7)])
+def test_modes_grid_runs_kernel(cuda, up, O, shape, elevation, seed):
+    """The x-coherent grid kernel of lakes, islands and legacy (run tables of
+    the lattice instances): every field mask, ragged runs and row tiles
+    (45 x 30 x 27), against the per-point kernel and the FP32 oracle."""
+    g = up.abi.Grid.make((-2000, -1900, -1800), (2000, 1900, 1800), (45, 30, 27))
+    planet = up.Planet(shape, elevation, "default", seed=seed)
+    pos = O.grid_positions(g)
+    pts = [planet.sdf_points(pos, field=f) for f in range(3)]
+    ref = O.Planet(shape, elevation, "default", seed=seed)
+    for mask in (1, 2, 4, 5, 7):
+        outs = planet.sdf_grid(g, mask)
+        for f in range(3):
+            if not (mask >> f) & 1:
+                continue
+            assert (_rel(outs[f], pts[f]) > 1e-5).mean() <= 1e-3, (mask, f)
+            assert (_rel(outs[f], ref.field(f, pos, precision=1)) > 1e-4).mean() <= 5e-3, (mask, f)

@@ -213,7 +213,7 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 		else {
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;
-			check(launch_modes_grid(ctx->d_modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream,
+			check(launch_modes_grid(ctx->d_modes, ctx->modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream,
 				modes_contour_band(ctx->modes, field, c.g.step)), "sdf grid kernel");
 		}
 		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
@@ -292,7 +292,7 @@ int sdf_grid_pipelined(up_context *ctx, uint32_t mask, const GridDev &g, float *
 			if (mask >> f & 1u) o[f] = stage[b] + (size_t)(q++) * cn;
 		float *dg = grad ? stage[b] + (size_t)nf * cn : nullptr;
 		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, gs, o[0], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
-		else check(launch_modes_grid(ctx->d_modes, mask, gs, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		else check(launch_modes_grid(ctx->d_modes, ctx->modes, mask, gs, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
 		check(cudaEventRecord(ctx->ev_done[b], ctx->stream), "cudaEventRecord");
 		check(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_done[b], 0), "cudaStreamWaitEvent");
 		const size_t off = plane * z0;
@@ -510,7 +510,7 @@ int up_sdf_grid(up_context *ctx, uint32_t mask, const up_grid *grid, float *cons
 		float *dg = (float *)stage_out(ctx, B_GRAD, grad, n * 12);
 		reset_flag(ctx);
 		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, g, o[0], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
-		else check(launch_modes_grid(ctx->d_modes, mask, g, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
+		else check(launch_modes_grid(ctx->d_modes, ctx->modes, mask, g, o[0], o[1], o[2], dg, ctx->d_flag, ctx->stream), "sdf grid kernel");
 		for (int f = 0; f < 3; f++)
 			if (mask >> f & 1u) finish_out(ctx, out[f], o[f], n * 4);
 		finish_out(ctx, grad, dg, n * 12);

@@ -388,9 +388,10 @@ UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename 
 template<bool GRAD, int T0, int T1>
 UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride, float band = 0.f) {
 	bool far = band > 0.f;
+	const uint32_t spheres = synth_segment_spheres(P, rc.px(0), rc.px(R - 1), rc.py, rc.pz);
 	#pragma unroll 1
 	for (int r = 0; r < R; r++) {
-		const NG b = synth_base<GRAD>(P, v3(rc.px(r), rc.py, rc.pz));
+		const NG b = synth_base<GRAD>(P, v3(rc.px(r), rc.py, rc.pz), spheres);
 		acc_set(acc, r * stride, b.v, b.g.x, b.g.y, b.g.z);
 		far = far && fabsf(b.v) > band;
 	}

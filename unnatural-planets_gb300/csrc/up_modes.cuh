@@ -400,40 +400,48 @@ template<class S> UP_HD_NOINLINE S shape_eval(const ModesDesc &M, V3S<S> pos) {
 }
 
 // ---------------------------------------------------------------- elevation modes
-template<class S> UP_HD S mountains(const ModesDesc &M, V3S<S> pos, S land) { // elevationModes.cpp:68-123
+// The elevation noise instances are read through a source NZ: nz(M, slot, pos)
+// returns noise_dev(M.elev[slot], pos) (NoiseDirect), or the same quantity
+// taken from a table that a grid kernel filled for a run of samples along x.
+struct NoiseDirect {
+	template<class S> UP_HD S operator()(const ModesDesc &M, int slot, V3S<S> pos) const { return noise_dev(M.elev[slot], pos); }
+};
+template<class S, class NZ> UP_HD S mountains(const ModesDesc &M, V3S<S> pos, S land, const NZ &nz) { // elevationModes.cpp:68-123
 	const S cover = 1.f - s_sat(land * -0.1f);
 	if (val(cover) < 1e-7f) return land;
-	const S mask = noise_dev(M.elev[NS_MTN_MASK], pos);
+	const S mask = nz(M, NS_MTN_MASK, pos);
 	const S rm = s_smoothstep(s_sat(mask * 7.f - 0.3f));
 	const S tm = s_smoothstep(s_sat(mask * -7.f - 1.5f));
-	S ridge = noise_dev(M.elev[NS_MTN_RIDGE], pos);
+	S ridge = nz(M, NS_MTN_RIDGE, pos);
 	ridge = s_max(ridge - 0.1f, mk<S>(0.f));
 	ridge = s_pow(ridge, 1.6f) * rm * cover * 1000.f;
-	S terraces = s_max(noise_dev(M.elev[NS_MTN_TERRACE], pos) + 0.1f, mk<S>(0.f)) * 2.5f;
+	S terraces = s_max(nz(M, NS_MTN_TERRACE, pos) + 0.1f, mk<S>(0.f)) * 2.5f;
 	terraces = s_terrace(terraces, 4.f) * tm * cover * 250.f;
 	return land + s_smax(mk<S>(0.f), s_max(ridge, terraces), 50.f);
 }
-template<class S> UP_HD_NOINLINE S elevation_eval(const ModesDesc &M, V3S<S> pos) {
-	switch (M.elevation) {
+// EM >= 0: the elevation mode is known at compile time (M.elevation == EM)
+template<class S, class NZ, int EM = -1> UP_HD S elevation_nz(const ModesDesc &M, V3S<S> pos, const NZ &nz) {
+	const int em = EM >= 0 ? EM : M.elevation;
+	switch (em) {
 		case 0: return mk<S>(100.f); // :9-12
 		case 1: { // :14-32
-			S a = -noise_dev(M.elev[NS_SIMPLE], pos) + 0.3f;
+			S a = -nz(M, NS_SIMPLE, pos) + 0.3f;
 			a = s_pow(a * 1.3f - 0.35f, 3.f) + 0.1f;
 			return 100.f - a * 1000.f;
 		}
 		case 2: { // :34-64
-			const S scale = noise_dev(M.elev[NS_LEGACY_SCALE], pos) * 0.0005f + 0.0015f;
+			const S scale = nz(M, NS_LEGACY_SCALE, pos) * 0.0005f + 0.0015f;
 			S a = noise_dev(M.elev[NS_LEGACY_ELEV], pos * scale) + 0.11f;
 			if (val(a) < 0.f) a = -s_pow(-a, 0.85f);
 			else a = s_pow(a, 1.7f);
 			return a * 2500.f;
 		}
 		case 3: case 4: { // lakes :129-149, islands :151-171
-			S land = s_sat(noise_dev(M.elev[M.elevation == 3 ? NS_LAKES_LAND : NS_ISLANDS_LAND], pos) * 0.5f + 0.5f);
-			land = 1.f - s_pow(land, M.elevation == 3 ? 1.24f : 0.83f);
+			S land = s_sat(nz(M, em == 3 ? NS_LAKES_LAND : NS_ISLANDS_LAND, pos) * 0.5f + 0.5f);
+			land = 1.f - s_pow(land, em == 3 ? 1.24f : 0.83f);
 			land = land * 2.f - 1.f;
 			land = (land / (s_abs(land) + 0.17f) + 0.15f) * 150.f;
-			return mountains(M, pos, land);
+			return mountains(M, pos, land, nz);
 		}
 		default: { // craters :173-198
 			const V3S<S> c = voronoi_nearest(M.craters, pos, (const V3f *)nullptr);
@@ -444,6 +452,7 @@ template<class S> UP_HD_NOINLINE S elevation_eval(const ModesDesc &M, V3S<S> pos
 		}
 	}
 }
+template<class S> UP_HD_NOINLINE S elevation_eval(const ModesDesc &M, V3S<S> pos) { return elevation_nz(M, pos, NoiseDirect{}); }
 
 // the five fields (modesConfiguration.cpp:230-279)
 template<class S> UP_HD S field_eval(const ModesDesc &M, int field, V3S<S> p) {

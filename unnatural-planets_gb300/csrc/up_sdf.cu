@@ -87,18 +87,20 @@ __global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_
 	const uint32_t nrows = ny * nz;
 	const uint32_t nruns = (nx + R - 1) / R;
 	const uint32_t tny = (ny + 7) / 8, tnz = (nz + 3) / 4;
-	const uint64_t ntasks = (uint64_t)nruns * tny * tnz;
+	// a task holds at least two samples of a grid of 2 .. 2^32 - 1 samples:
+	// ntasks < 2^31, and t + nwarps below cannot wrap
+	const uint32_t ntasks = nruns * tny * tnz;
 	const uint64_t plane = (uint64_t)nx * nrows;
 	const uint32_t lane = threadIdx.x & 31;
-	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
 	runs_tables_init();
 	RunCtx rc;
 	rc.lo_x = g.lo[0];
 	rc.step_x = g.step[0];
 	rc.nx = nx;
 	bool bad = false;
-	for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nwarps) {
-		const uint32_t run = (uint32_t)(t % nruns), tile = (uint32_t)(t / nruns);
+	for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nwarps) {
+		const uint32_t run = t % nruns, tile = t / nruns;
 		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
 		const bool live = jr < ny && kr < nz;
 		const uint32_t j = jr < ny ? jr : ny - 1, k = kr < nz ? kr : nz - 1;

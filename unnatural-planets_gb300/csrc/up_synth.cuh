@@ -87,8 +87,18 @@ UP_HD NG box_d(V3f p, float h, float rr) {
 	return ng(ml + fminf(mx, 0.f) - rr, g);
 }
 
+UP_HD int lowest_bit(uint32_t m) {
+#ifdef __CUDA_ARCH__
+	return __ffs(m) - 1;
+#else
+	return __builtin_ctz(m);
+#endif
+}
+
+// spheres: bit s clear = sphere s is known to be skipped at p (the test
+// below would skip it; synth_segment_spheres); the others are tested
 template<bool GRAD>
-UP_HD NG synth_base(const up_synth_program &P, V3f p) {
+UP_HD NG synth_base(const up_synth_program &P, V3f p, uint32_t spheres = 0xFFFFFFFFu) {
 	switch (P.base) {
 		case UP_BASE_SPHERE: return sphere_d(p, zero3(), P.param[0]);
 		case UP_BASE_TORUS: return torus_d(p, P.param[0], P.param[1]);
@@ -96,8 +106,10 @@ UP_HD NG synth_base(const up_synth_program &P, V3f p) {
 		default: {
 			NG b = torus_d(p, P.param[0], P.param[1]);
 			const float ik = 1.f / P.k;
+			// in increasing s, as the union is defined
 			#pragma unroll 1
-			for (int s = 0; s < P.n_spheres; s++) {
+			for (uint32_t live = spheres & ((1u << P.n_spheres) - 1u); live != 0u; live &= live - 1u) {
+				const int s = lowest_bit(live);
 				const V3f c = v3(P.sphere[s][0], P.sphere[s][1], P.sphere[s][2]);
 				// A sphere at distance l >= radius + b + k leaves the blend
 				// weight saturated (h = 1): the smooth minimum returns b and
@@ -113,6 +125,34 @@ UP_HD NG synth_base(const up_synth_program &P, V3f p) {
 			return b;
 		}
 	}
+}
+
+// Spheres of a torus-spheres union that can change it somewhere on the
+// segment of samples (x, y, z), x in [x0, x1]: every sphere whose bit is
+// clear is skipped by synth_base's own test at every sample of the segment.
+// That test skips sphere s at p when |p - c_s|^2 >= lim^2 (or lim <= 0),
+// lim = r_s + b + 1.001 k + 1e-6, with b the union so far. b never exceeds
+// the torus (the smooth minimum is below both arguments), and the torus is
+// 1-Lipschitz, so b <= torus(midpoint) + half the segment; with that bound
+// in lim and the segment's nearest point to c_s in |p - c_s|, the margins
+// (relative 1e-5 on the bound, 1e-4 on the squares) cover FP32 rounding.
+UP_HD uint32_t synth_segment_spheres(const up_synth_program &P, float x0, float x1, float y, float z) {
+	if (P.base != UP_BASE_TORUS_SPHERES) return 0xFFFFFFFFu;
+	const float xm = 0.5f * (x0 + x1), half = 0.5f * (x1 - x0);
+	const float tm = torus_d(v3(xm, y, z), P.param[0], P.param[1]).v;
+	const float bmax = tm + half + 1e-5f * (1.f + fabsf(tm) + fabsf(xm) + fabsf(y) + fabsf(z) + half);
+	uint32_t live = 0u;
+	#pragma unroll 1
+	for (int s = 0; s < P.n_spheres; s++) {
+		const float L = P.sphere[s][3] + bmax + P.k * 1.001f + 1e-6f;
+		if (L <= 0.f) continue;
+		const float cx = P.sphere[s][0];
+		const float dx = fmaxf(fmaxf(x0 - cx, cx - x1), 0.f), dy = y - P.sphere[s][1], dz = z - P.sphere[s][2];
+		const float d2 = dx * dx + dy * dy + dz * dz;
+		if (d2 >= L * L * 1.0001f + 1e-9f) continue;
+		live |= 1u << s;
+	}
+	return live;
 }
 
 // Upper bounds of |n| per noise type, from the definitions in up_noise.cuh:
