@@ -149,16 +149,26 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 		for (int h = 0; h < 2; h++) {
 			if (h == 0 && carry) continue;
 			const uint32_t xh = (uint32_t)(cx + h) * HX;
-			float gxs = 0.f, cs = 0.f, pys = 0.f, qys = 0.f, pzs = 0.f, qzs = 0.f;
+			float4 cg[4]; // corner c: gradient vector, or the value in .x
 			#pragma unroll
 			for (int c = 0; c < 4; c++) {
 				const uint32_t hh = mix32(xh ^ yz[c]);
 				if (VALUE) {
-					const float val = hash_signed(hh);
+					cg[c].x = hash_signed(hh);
+				} else {
+					const V3f g = grad_lookup(hh);
+					cg[c].x = g.x; cg[c].y = g.y; cg[c].z = g.z;
+				}
+			}
+			float gxs = 0.f, cs = 0.f, pys = 0.f, qys = 0.f, pzs = 0.f, qzs = 0.f;
+			#pragma unroll
+			for (int c = 0; c < 4; c++) {
+				if (VALUE) {
+					const float val = cg[c].x;
 					cs += Wyz[c] * val;
 					if (GRAD) { qys += dWy[c] * val; qzs += dWz[c] * val; }
 				} else {
-					const V3f g = grad_lookup(hh);
+					const V3f g = v3(cg[c].x, cg[c].y, cg[c].z);
 					const float cyz = g.y * ys[c] + g.z * zs[c];
 					gxs += Wyz[c] * g.x;
 					cs += Wyz[c] * cyz;
@@ -202,9 +212,10 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 // at compile time. Returns false (nothing accumulated) when the sub-run spans
 // more than two x cells; the caller then evaluates those samples one by one.
 // The x cells are the same for every lane. A candidate is ranked by its
-// distance with the low 6 mantissa bits replaced by its id (column * 9 + yz):
-// the two smallest keys per sample are kept with integer min/max, and the
-// winners' exact distances and difference vectors are rebuilt from the ids.
+// distance with the low 6 mantissa bits replaced by its id
+// col * 16 + (dy + 1) * 4 + (dz + 1): the two smallest keys per sample are
+// kept with integer min/max, and the winners' exact distances and difference
+// vectors are rebuilt from the ids.
 UP_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
 UP_HD uint32_t umax32(uint32_t a, uint32_t b) { return a > b ? a : b; }
 template<int DIST>
@@ -217,8 +228,9 @@ UP_HD float cell_metric(float vx, float e2yz, float m1yz) {
 // z cells span at most two values each, the union of their 3x3 neighbourhoods
 // times the sub-run's columns fits a 4 x 4 x 4 table that the lanes hash
 // together (two cells each) and every lane reads (broadcasts); otherwise each
-// lane hashes its own candidates. Entry (col, yy, zz) at (col * 4 + yy) * 4 + zz
-// holds the cell's jitter and hash.
+// lane hashes its own candidates. Entry (col, yy, zz) at col * 16 + yy * 4 + zz
+// holds the cell's jitter and hash, so a lane's candidate with id
+// col * 16 + (dy + 1) * 4 + (dz + 1) sits at id + (ty - 1) * 4 + (tz - 1).
 struct CellEntry { float jx, jy, jz; uint32_t h; };
 constexpr int CT = 4;
 #ifdef __CUDACC__
@@ -259,30 +271,30 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 	#pragma unroll
 	for (int r = 0; r < S; r++) { K1[r] = 0xFFFFFFFFu; K2[r] = 0xFFFFFFFFu; }
 	const int ncol = ixb - ixa + 3;
-	int ty = 0, tz = 0; // this lane's offsets into the shared table
+	int off = 0; // table index of candidate id: id + off
 	bool table = false;
 #ifdef __CUDA_ARCH__
 	const int iymin = __reduce_min_sync(0xFFFFFFFFu, iy), iymax = __reduce_max_sync(0xFFFFFFFFu, iy);
 	const int izmin = __reduce_min_sync(0xFFFFFFFFu, iz), izmax = __reduce_max_sync(0xFFFFFFFFu, iz);
 	table = iymax - iymin <= 1 && izmax - izmin <= 1; // the same for every lane
-	CellEntry *ct = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
+	const CellEntry *ct = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
 	if (table) {
+		CellEntry *w = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
 		__syncwarp(); // the previous sub-run's readers are done
-		for (int e = (int)(threadIdx.x & 31); e < ncol * CT * CT; e += 32) {
-			const int col = e / (CT * CT), yy = (e / CT) % CT, zz = e % CT;
-			ct[e] = cell_entry(mix32(((uint32_t)(ixa - 1 + col) * HX) ^ ((uint32_t)(iymin - 1 + yy) * HY) ^ (((uint32_t)(izmin - 1 + zz) * HZ) ^ key)));
-		}
+		for (int e = (int)(threadIdx.x & 31); e < ncol * CT * CT; e += 32)
+			w[e] = cell_entry(mix32(((uint32_t)(ixa - 1 + (e >> 4)) * HX) ^ ((uint32_t)(iymin - 1 + ((e >> 2) & 3)) * HY) ^
+				(((uint32_t)(izmin - 1 + (e & 3)) * HZ) ^ key)));
 		__syncwarp();
-		ty = iy - iymin + 1;
-		tz = iz - izmin + 1;
+		off = (iy - iymin) * CT + (iz - izmin);
 	}
 #endif
-	// candidate cell (column col, neighbour dy, dz) of this lane
-	auto cand = [&](int col, int dy, int dz) -> CellEntry {
+	// candidate cell with id (column, dy + 1, dz + 1) of this lane
+	auto cand = [&](int id) -> CellEntry {
 #ifdef __CUDA_ARCH__
-		if (table) return ct[(col * CT + ty + dy) * CT + tz + dz];
+		if (table) return ct[id + off];
 #endif
-		return cell_entry(mix32(((uint32_t)(ixa - 1 + col) * HX) ^ ((uint32_t)(iy + dy) * HY) ^ (((uint32_t)(iz + dz) * HZ) ^ key)));
+		return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
+			(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)));
 	};
 	#pragma unroll 1
 	for (int col = 0; col < ncol; col++) {
@@ -292,19 +304,22 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
 		const float fcol = (float)(col - 1);
 		#pragma unroll 1
-		for (int yz = 0; yz < 9; yz++) {
-			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
-			const CellEntry ce = cand(col, dy, dz);
-			const float vy = ((float)dy + ce.jy) - fy;
-			const float vz = ((float)dz + ce.jz) - fz;
-			const float T = fcol + ce.jx;
-			const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
-			const uint32_t id = (uint32_t)(col * 9 + yz);
+		for (int dy = -1; dy <= 1; dy++) {
+			const float fdy = (float)dy;
 			#pragma unroll
-			for (int r = 0; r < S; r++) {
-				const uint32_t k = (f_bits(cell_metric<DIST>(T - sc[r], e2yz, m1yz)) & ~63u) | id;
-				K2[r] = umin32(K2[r], umax32(K1[r], k));
-				K1[r] = umin32(K1[r], k);
+			for (int dz = -1; dz <= 1; dz++) {
+				const uint32_t id = (uint32_t)(col * 16 + (dy + 1) * 4 + (dz + 1));
+				const CellEntry ce = cand((int)id);
+				const float vy = (fdy + ce.jy) - fy;
+				const float vz = ((float)dz + ce.jz) - fz;
+				const float T = fcol + ce.jx;
+				const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
+				#pragma unroll
+				for (int r = 0; r < S; r++) {
+					const uint32_t k = (f_bits(cell_metric<DIST>(T - sc[r], e2yz, m1yz)) & ~63u) | id;
+					K2[r] = umin32(K2[r], umax32(K1[r], k));
+					K1[r] = umin32(K1[r], k);
+				}
 			}
 		}
 	}
@@ -315,13 +330,11 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		uint32_t h1 = 0;
 		#pragma unroll
 		for (int wsel = 0; wsel < 2; wsel++) {
-			const uint32_t id = (wsel ? K2[r] : K1[r]) & 63u;
-			const int col = (int)(id / 9u), yz = (int)(id % 9u);
-			const int dy = yz / 3 - 1, dz = yz % 3 - 1;
-			const CellEntry ce = cand(col, dy, dz);
-			const float vy = ((float)dy + ce.jy) - fy;
-			const float vz = ((float)dz + ce.jz) - fz;
-			const float vx = ((float)(col - 1) + ce.jx) - sx[r];
+			const int id = (int)((wsel ? K2[r] : K1[r]) & 63u);
+			const CellEntry ce = cand(id);
+			const float vy = ((float)(((id >> 2) & 3) - 1) + ce.jy) - fy;
+			const float vz = ((float)((id & 3) - 1) + ce.jz) - fz;
+			const float vx = ((float)((id >> 4) - 1) + ce.jx) - sx[r];
 			const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
 			Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
 			vw[wsel] = v3(vx, vy, vz);

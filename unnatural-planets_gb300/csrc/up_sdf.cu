@@ -75,8 +75,11 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 // acc[r * RUNS_T + t]
 constexpr int RUNS_T = 128;
 static_assert(RUNS_T == 32 * RUNS_WARPS, "the x tables of up_grid_runs.cuh hold one row per warp");
+// 6 blocks per SM: the value + gradient form's shared memory (32 KiB of
+// accumulators plus the tables) admits 6, and the cap keeps the registers
+// (80) from admitting fewer; caps of 5, 7 and 8 timed slower
 template<bool GRAD, int T0, int T1>
-__global__ void __launch_bounds__(RUNS_T) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
+__global__ void __launch_bounds__(RUNS_T, 6) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
 	float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
 	typedef typename AccOf<GRAD>::T A;
 	extern __shared__ __align__(16) unsigned char runs_smem[];
