@@ -149,16 +149,11 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 		for (int h = 0; h < 2; h++) {
 			if (h == 0 && carry) continue;
 			const uint32_t xh = (uint32_t)(cx + h) * HX;
-			float4 cg[4]; // corner c: gradient vector, or the value in .x
+			V3f cg[4]; // corner c: gradient vector, or the value in .x
 			#pragma unroll
 			for (int c = 0; c < 4; c++) {
 				const uint32_t hh = mix32(xh ^ yz[c]);
-				if (VALUE) {
-					cg[c].x = hash_signed(hh);
-				} else {
-					const V3f g = grad_lookup(hh);
-					cg[c].x = g.x; cg[c].y = g.y; cg[c].z = g.z;
-				}
+				cg[c] = VALUE ? v3(hash_signed(hh), 0.f, 0.f) : grad_lookup(hh);
 			}
 			float gxs = 0.f, cs = 0.f, pys = 0.f, qys = 0.f, pzs = 0.f, qzs = 0.f;
 			#pragma unroll
@@ -168,7 +163,7 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 					cs += Wyz[c] * val;
 					if (GRAD) { qys += dWy[c] * val; qzs += dWz[c] * val; }
 				} else {
-					const V3f g = v3(cg[c].x, cg[c].y, cg[c].z);
+					const V3f g = cg[c];
 					const float cyz = g.y * ys[c] + g.z * zs[c];
 					gxs += Wyz[c] * g.x;
 					cs += Wyz[c] * cyz;
