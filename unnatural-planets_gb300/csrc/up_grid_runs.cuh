@@ -79,7 +79,7 @@ UP_HD V3f grad_lookup(uint32_t h) {
 // once per octave and all lanes read it (shared-memory broadcast) instead of
 // each forming x, floor, fade and fade' per sample.
 struct XTab { float fx, u, du; int cx; };
-constexpr int RUNS_WARPS = 4; // warps per block of the runs kernel
+constexpr int RUNS_WARPS = 8; // warps per block of the runs kernels
 #ifdef __CUDACC__
 __shared__ XTab g_runs_xtab[RUNS_WARPS * RUN_R];
 #endif

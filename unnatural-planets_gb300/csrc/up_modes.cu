@@ -70,7 +70,7 @@ constexpr int MRUNS_T = 32 * RUNS_WARPS;
 constexpr int MRUN_SLOTS = 4; // slots 0-2: noise instances, then the three fields (in place); 3: shape values
 
 template<int EM>
-__global__ void __launch_bounds__(MRUNS_T) modes_grid_runs_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g,
+__global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g,
 	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, unsigned *__restrict__ nanflag, float band) {
 	extern __shared__ __align__(16) float mruns_smem[];
 	constexpr int R = RUN_R;
@@ -184,8 +184,9 @@ static cudaError_t launch_p(K kernel, uint64_t work, cudaStream_t s, A... args) 
 
 template<class K, class... A>
 static cudaError_t launch_mruns(K kernel, const GridDev &g, cudaStream_t s, A... args) {
-	constexpr size_t smem = (size_t)MRUN_SLOTS * RUN_R * MRUNS_T * sizeof(float); // 32 KiB
-	static_assert(smem <= 48 * 1024, "run tables exceed the default shared-memory limit");
+	constexpr size_t smem = (size_t)MRUN_SLOTS * RUN_R * MRUNS_T * sizeof(float); // 64 KiB
+	const cudaError_t e = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
 	uint64_t blocks = (uint64_t)persistent_blocks((const void *)kernel, MRUNS_T, smem);
 	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
 	const uint64_t need = (tasks + MRUNS_T / 32 - 1) / (MRUNS_T / 32);

@@ -73,13 +73,14 @@ __global__ void __launch_bounds__(256) synth_grid_kernel(const up_synth_program 
 // noise more often under the narrow band of contouring); accumulators in
 // dynamic shared memory, RUNS_T slots per sample index, so thread t owns
 // acc[r * RUNS_T + t]
-constexpr int RUNS_T = 128;
+constexpr int RUNS_T = 256;
 static_assert(RUNS_T == 32 * RUNS_WARPS, "the x tables of up_grid_runs.cuh hold one row per warp");
-// 6 blocks per SM: the value + gradient form's shared memory (32 KiB of
-// accumulators plus the tables) admits 6, and the cap keeps the registers
-// (80) from admitting fewer; caps of 5, 7 and 8 timed slower
+// 3 blocks of 8 warps per SM: the value + gradient form's shared memory
+// (64 KiB of accumulators plus 10 KiB of tables per block) admits 3, and the
+// cap keeps the registers (80) from admitting fewer. Timed against 4-warp
+// blocks (5 per SM, shared-memory bound: 5.25 ms at 512^3) and 2-warp blocks.
 template<bool GRAD, int T0, int T1>
-__global__ void __launch_bounds__(RUNS_T, 6) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
+__global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
 	float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
 	typedef typename AccOf<GRAD>::T A;
 	extern __shared__ __align__(16) unsigned char runs_smem[];
@@ -202,9 +203,10 @@ static cudaError_t launch_persistent(K kernel, uint64_t work, cudaStream_t s, A.
 
 template<bool GRAD, class K, class... A>
 static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, A... args) {
-	// 32 KiB (value + gradient) or 8 KiB: below the 48 KiB default limit
+	// 64 KiB (value + gradient) or 16 KiB of accumulators
 	constexpr size_t smem = (size_t)RUN_R * RUNS_T * sizeof(typename AccOf<GRAD>::T);
-	static_assert(smem <= 48 * 1024, "runs accumulators exceed the default shared-memory limit");
+	const cudaError_t e = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
 	uint64_t blocks = (uint64_t)persistent_blocks((const void *)kernel, RUNS_T, smem);
 	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
 	const uint64_t need = (tasks + RUNS_T / 32 - 1) / (RUNS_T / 32);
