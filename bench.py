@@ -317,8 +317,21 @@ def extra_fit(up, W, stream, steps=300):
     planet.set_theta(theta.detach().cpu().numpy())
     fit = planet.sdf_points(xs)
     ref = O.synth_points(P, xs, theta=t_star_np.astype(np.float64))
+    # relative error per parameter group (layout of workloads.theta_of)
+    amp_i, freq_i, o = [], [], 0
+    for l in range(P.n_layers):
+        k = P.layer[l].octaves
+        amp_i += list(range(o, o + k))
+        freq_i += list(range(o + k, o + 2 * k))
+        o += 2 * k
+    groups = {"amplitudes": amp_i, "frequencies": freq_i, "shape": list(range(o, len(t_star_np)))}
+
+    def group_err(t):
+        t = np.asarray(t, np.float64)
+        return {g: float(np.linalg.norm(t[i] - t_star_np[i]) / np.linalg.norm(t_star_np[i])) for g, i in groups.items()}
     return {"steps": steps, "ms_per_step": ms, "points": n, "sign_points": int(xg.shape[0]), "loss": float(loss.detach()),
             "theta_rel_err_start": err0, "theta_rel_err_end": float((theta.detach() - t_star).norm() / t_star.norm()),
+            "theta_rel_err_by_group_start": group_err(t0), "theta_rel_err_by_group_end": group_err(theta.detach().cpu().numpy()),
             "sdf_rms_vs_fp64_oracle": float(np.sqrt(np.mean((fit - ref) ** 2))),
             "what": "torus + 8 spheres - ridged perlin + cellular, 25 parameters; theta* = theta (1 + 0.05 U) seed 1, "
                     "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell + "

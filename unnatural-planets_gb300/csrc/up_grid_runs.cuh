@@ -223,32 +223,37 @@ UP_HD float cell_metric(float vx, float e2yz, float m1yz) {
 // z cells span at most two values each, the union of their 3x3 neighbourhoods
 // times the sub-run's columns fits a 4 x 4 x 4 table that the lanes hash
 // together (two cells each) and every lane reads (broadcasts); otherwise each
-// lane hashes its own candidates. Entry (col, yy, zz) at col * 16 + yy * 4 + zz
-// holds the cell's jitter and hash, so a lane's candidate with id
-// col * 16 + (dy + 1) * 4 + (dz + 1) sits at id + (ty - 1) * 4 + (tz - 1).
+// lane hashes its own candidates. Entry e = col * 16 + yy * 4 + zz holds the
+// cell's feature point relative to the table's corner cell (col - 1 + jx,
+// yy + jy, zz + jz; exact in FP32) and its hash, so a lane's candidate with id
+// col * 16 + (dy + 1) * 4 + (dz + 1) sits at id + (ty - 1) * 4 + (tz - 1) and
+// its offset is (jy - ty) - fy along y (lane mode: the lane's own 3 x 3 x 3
+// block is the table, ty = 1).
 struct CellEntry { float jx, jy, jz; uint32_t h; };
 constexpr int CT = 4;
 #ifdef __CUDACC__
 __shared__ CellEntry g_runs_cells[RUNS_WARPS * CT * CT * CT];
 #endif
-UP_HD CellEntry cell_entry(uint32_t h) {
+UP_HD CellEntry cell_entry(uint32_t h, int e) {
 	CellEntry c;
-	c.jx = jitter(h, 0);
-	c.jy = jitter(h, 10);
-	c.jz = jitter(h, 20);
+	c.jx = (float)((e >> 4) - 1) + jitter(h, 0);
+	c.jy = (float)((e >> 2) & 3) + jitter(h, 10);
+	c.jz = (float)(e & 3) + jitter(h, 20);
 	c.h = h;
 	return c;
 }
 
+// tab: the run's x table at frequency f (xtab_entry, shared by the warp)
 template<bool GRAD, int DIST, int OP>
-UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
+UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, float amp, bool ridged, uint32_t key,
+	typename AccOf<GRAD>::T *acc, int stride) {
 	constexpr int S = CELL_SUB;
 	const float qy = rc.py * f, qz = rc.pz * f;
 	const float fy0 = floorf(qy), fz0 = floorf(qz);
 	const int iy = (int)fy0, iz = (int)fz0;
 	const float fy = qy - fy0, fz = qz - fz0;
-	const int ixa = (int)floorf(rc.px(r0) * f);
-	const int ixb = (int)floorf(rc.px(r0 + S - 1) * f);
+	const int ixa = tab[r0].cx;
+	const int ixb = tab[r0 + S - 1].cx;
 	if (ixb - ixa > 1) return false;
 	// sx[r] = (ix_r - ixa) + fx_r: then x difference to a candidate in column
 	// cxi = ixa - 1 + col is ((col - 1) + jitter) - sx[r]
@@ -256,10 +261,9 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 	int split = S; // samples [0, split) are in cell ixa, the rest in ixa + 1
 	#pragma unroll
 	for (int r = S - 1; r >= 0; r--) {
-		const float qx = rc.px(r0 + r) * f;
-		const float fx0 = floorf(qx);
-		const bool second = (int)fx0 != ixa;
-		sx[r] = second ? 1.f + (qx - fx0) : qx - fx0;
+		const XTab e = tab[r0 + r];
+		const bool second = e.cx != ixa;
+		sx[r] = second ? 1.f + e.fx : e.fx;
 		if (second) split = r;
 	}
 	uint32_t K1[S], K2[S];
@@ -267,6 +271,7 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 	for (int r = 0; r < S; r++) { K1[r] = 0xFFFFFFFFu; K2[r] = 0xFFFFFFFFu; }
 	const int ncol = ixb - ixa + 3;
 	int off = 0; // table index of candidate id: id + off
+	int ty = 1, tz = 1; // table cell of this lane's own cell
 	bool table = false;
 #ifdef __CUDA_ARCH__
 	const int iymin = __reduce_min_sync(0xFFFFFFFFu, iy), iymax = __reduce_max_sync(0xFFFFFFFFu, iy);
@@ -278,9 +283,11 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		__syncwarp(); // the previous sub-run's readers are done
 		for (int e = (int)(threadIdx.x & 31); e < ncol * CT * CT; e += 32)
 			w[e] = cell_entry(mix32(((uint32_t)(ixa - 1 + (e >> 4)) * HX) ^ ((uint32_t)(iymin - 1 + ((e >> 2) & 3)) * HY) ^
-				(((uint32_t)(izmin - 1 + (e & 3)) * HZ) ^ key)));
+				(((uint32_t)(izmin - 1 + (e & 3)) * HZ) ^ key)), e);
 		__syncwarp();
 		off = (iy - iymin) * CT + (iz - izmin);
+		ty = iy - iymin + 1;
+		tz = iz - izmin + 1;
 	}
 #endif
 	// candidate cell with id (column, dy + 1, dz + 1) of this lane
@@ -289,25 +296,24 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		if (table) return ct[id + off];
 #endif
 		return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
-			(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)));
+			(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)), id);
 	};
+	const float tyf = (float)ty, tzf = (float)tz;
 	#pragma unroll 1
 	for (int col = 0; col < ncol; col++) {
 		// a column outside a sample's 3x3x3 neighbourhood is pushed far away
 		float sc[S];
 		#pragma unroll
 		for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
-		const float fcol = (float)(col - 1);
 		#pragma unroll 1
 		for (int dy = -1; dy <= 1; dy++) {
-			const float fdy = (float)dy;
 			#pragma unroll
 			for (int dz = -1; dz <= 1; dz++) {
 				const uint32_t id = (uint32_t)(col * 16 + (dy + 1) * 4 + (dz + 1));
 				const CellEntry ce = cand((int)id);
-				const float vy = (fdy + ce.jy) - fy;
-				const float vz = ((float)dz + ce.jz) - fz;
-				const float T = fcol + ce.jx;
+				const float vy = (ce.jy - tyf) - fy;
+				const float vz = (ce.jz - tzf) - fz;
+				const float T = ce.jx;
 				const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
 				#pragma unroll
 				for (int r = 0; r < S; r++) {
@@ -327,9 +333,9 @@ UP_HD bool cellular_subrun(const RunCtx &rc, int r0, float f, float amp, bool ri
 		for (int wsel = 0; wsel < 2; wsel++) {
 			const int id = (int)((wsel ? K2[r] : K1[r]) & 63u);
 			const CellEntry ce = cand(id);
-			const float vy = ((float)(((id >> 2) & 3) - 1) + ce.jy) - fy;
-			const float vz = ((float)((id & 3) - 1) + ce.jz) - fz;
-			const float vx = ((float)((id >> 4) - 1) + ce.jx) - sx[r];
+			const float vy = (ce.jy - tyf) - fy;
+			const float vz = (ce.jz - tzf) - fz;
+			const float vx = ce.jx - sx[r];
 			const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
 			Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
 			vw[wsel] = v3(vx, vy, vz);
@@ -373,9 +379,18 @@ UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename 
 		else if (TYPE == 2) lattice_octave_run<GRAD, false>(rc, R, f, a, ridged, key, acc, stride);
 		else {
 			constexpr int DIST = ((TYPE >> 4) & 15) - 1, OP = ((TYPE >> 8) & 15) - 1;
+#ifdef __CUDA_ARCH__
+			XTab *tab = g_runs_xtab + (threadIdx.x >> 5) * RUN_R;
+			__syncwarp(); // every lane has finished reading the previous table
+			if ((int)(threadIdx.x & 31) < R) tab[threadIdx.x & 31] = xtab_entry(rc, (int)(threadIdx.x & 31), f);
+			__syncwarp();
+#else
+			XTab tab[RUN_R];
+			for (int q = 0; q < R; q++) tab[q] = xtab_entry(rc, q, f);
+#endif
 			#pragma unroll 1
 			for (int r0 = 0; r0 < R; r0 += CELL_SUB) {
-				if (cellular_subrun<GRAD, DIST, OP>(rc, r0, f, a, ridged, key, acc, stride)) continue;
+				if (cellular_subrun<GRAD, DIST, OP>(rc, tab, r0, f, a, ridged, key, acc, stride)) continue;
 				#pragma unroll 1
 				for (int r = r0; r < r0 + CELL_SUB; r++) {
 					const NG n = cellular_n<GRAD, DIST, OP>(v3(rc.px(r) * f, rc.py * f, rc.pz * f), key, DIST, OP);
