@@ -5,6 +5,7 @@
 // FP32, one thread per texel or tile.
 #pragma once
 #include "up_modes.cuh"
+#include "up_synth.cuh"
 
 namespace up {
 
@@ -415,7 +416,9 @@ UP_HD_NOINLINE void color_tile(const ModesDesc &M, TileD &t) { Colorer{M}.pipeli
 
 // synthetic texel program: albedo from 3-octave value noise (freq 4),
 // roughness from 2-octave simplex noise (freq 8), height = 0.5 + elevation /
-// (2 sum|amp|); seeds offset from the first layer's seed by 100 and 200
+// (2 sum|amp|); seeds offset from the first layer's seed by 100 and 200.
+// T0/T1: compile-time noise type of layer 0/1 (noise_t; -1 = run time)
+template<int T0 = -1, int T1 = -1>
 UP_HD void synth_texel(const up_synth_program &P, V3f p, V3f &albedo, float &rough, float &height) {
 	const uint32_t s0 = P.n_layers > 0 ? P.layer[0].seed : 0u;
 	float a = 0.f, r = 0.f;
@@ -430,9 +433,11 @@ UP_HD void synth_texel(const up_synth_program &P, V3f p, V3f &albedo, float &rou
 	float tot = 0.f, e = 0.f;
 	for (int l = 0; l < P.n_layers; l++) {
 		const up_noise_layer &L = P.layer[l];
+		#pragma unroll 1
 		for (int i = 0; i < L.octaves; i++) {
 			tot += fabsf(L.amp[i]);
-			float v = noise_single<false>(L.type, p * L.freq[i], seed_key(L.seed + (uint32_t)i), L.distance, L.operation).v;
+			const uint32_t key = seed_key(L.seed + (uint32_t)i);
+			float v = l == 0 ? noise_t<false, T0>(L, p * L.freq[i], key).v : noise_t<false, T1>(L, p * L.freq[i], key).v;
 			if (L.fractal == UP_FRACTAL_RIDGED) v = 1.f - 2.f * fabsf(v);
 			e += v * L.amp[i];
 		}

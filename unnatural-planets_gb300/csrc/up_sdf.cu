@@ -179,17 +179,6 @@ __global__ void __launch_bounds__(256) synth_points_kernel(const up_synth_progra
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
 }
 
-// Specialisations: the two benchmark programs get compile-time noise types;
-// everything else dispatches on the layer type at run time.
-enum Spec { SPEC_PERLIN_CELL = 0, SPEC_SIMPLEX = 1, SPEC_GENERIC = 2 };
-constexpr int CELL_EU_SUB = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);
-static Spec spec_of(const up_synth_program &P) {
-	if (P.n_layers == 2 && P.layer[0].type == UP_NOISE_PERLIN && P.layer[1].type == UP_NOISE_CELLULAR &&
-		P.layer[1].distance == UP_DIST_EUCLIDEAN && P.layer[1].operation == UP_OP_SUBTRACT)
-		return SPEC_PERLIN_CELL;
-	if (P.n_layers == 1 && P.layer[0].type == UP_NOISE_SIMPLEX) return SPEC_SIMPLEX;
-	return SPEC_GENERIC;
-}
 
 template<class K, class... A>
 static cudaError_t launch_persistent(K kernel, uint64_t work, cudaStream_t s, A... args) {

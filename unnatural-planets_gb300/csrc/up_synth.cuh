@@ -25,6 +25,18 @@ UP_HD NG noise_t(const up_noise_layer &L, V3f q, uint32_t key) {
 	return noise_single<GRAD>(t, q, key, L.distance, L.operation);
 }
 
+// Specialisations: the two benchmark programs get compile-time noise types;
+// everything else dispatches on the layer type at run time.
+enum Spec { SPEC_PERLIN_CELL = 0, SPEC_SIMPLEX = 1, SPEC_GENERIC = 2 };
+constexpr int CELL_EU_SUB = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);
+inline Spec spec_of(const up_synth_program &P) {
+	if (P.n_layers == 2 && P.layer[0].type == UP_NOISE_PERLIN && P.layer[1].type == UP_NOISE_CELLULAR &&
+		P.layer[1].distance == UP_DIST_EUCLIDEAN && P.layer[1].operation == UP_OP_SUBTRACT)
+		return SPEC_PERLIN_CELL;
+	if (P.n_layers == 1 && P.layer[0].type == UP_NOISE_SIMPLEX) return SPEC_SIMPLEX;
+	return SPEC_GENERIC;
+}
+
 // one layer: value and gradient with respect to p
 template<bool GRAD, int TYPE>
 UP_HD NG layer_eval(const up_noise_layer &L, V3f p) {

@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(256) tex_raster_kernel(const TexMesh m, uint32
 }
 
 // per texel: interpolate position and normal of the owning triangle, color
-template<bool SYNTH>
+// T0/T1: compile-time noise types of the synthetic program's layers (synth_texel)
+template<bool SYNTH, int T0 = -1, int T1 = -1>
 __global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_t W, uint32_t H, const int *__restrict__ owner,
 	const ModesDesc *__restrict__ Mp, const up_synth_program P, int purpose, float *__restrict__ img, int ach) {
 	const int nch = ach + 3;
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_
 		V3f albedo;
 		float rough, metal = 0.f, height, opacity = 1.f;
 		if (SYNTH) {
-			synth_texel(P, pf, albedo, rough, height);
+			synth_texel<T0, T1>(P, pf, albedo, rough, height);
 		} else {
 			TileD tl = tile_init(pf, nf, purpose);
 			color_tile(*Mp, tl);
@@ -162,35 +163,58 @@ __device__ __forceinline__ uint8_t to_u8(float v) { return isnan(v) ? (uint8_t)0
 // valid (0 = covered, DT_ABSENT = outside the image, DT_NAN = not yet), and
 // round k fills a NaN texel from the neighbours with tag < k (the texels
 // valid before round k, exactly those tex_dilate_kernel reads), so texels
-// filled in round k are not read in round k. Round k updates the region k
-// texels in from the loaded edge. Same arithmetic and neighbour order as
-// tex_dilate_kernel.
+// filled in round k are not read in round k, and the order in which a round
+// visits its texels does not matter. Round k updates the region k texels in
+// from the loaded edge. The rounds visit only the tile's NaN texels (a list
+// built while loading; a tile without any skips the rounds). Same arithmetic
+// and neighbour order as tex_dilate_kernel. RT > 0: the round count is RT at
+// compile time (the reference's 7), else `rounds`.
 constexpr int DT_X = 32, DT_Y = 16, DT_MAX_ROUNDS = 16;
 constexpr uint8_t DT_ABSENT = 254, DT_NAN = 255;
 __host__ __device__ inline size_t dilate_smem(int rounds, int nch) {
 	const size_t t = (size_t)(DT_X + 2 * rounds) * (DT_Y + 2 * rounds);
-	return sizeof(float) * t * nch + ((t + 15) & ~(size_t)15);
+	return sizeof(float) * t * nch + ((t + 15) & ~(size_t)15) + sizeof(uint32_t) * t;
 }
-__global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__restrict__ img, uint32_t W, uint32_t H, int nch, int ach, int rounds,
+template<int RT>
+__global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__restrict__ img, uint32_t W, uint32_t H, int nch, int ach, int rounds_rt,
 	uint8_t *__restrict__ a8, uint8_t *__restrict__ s8, uint8_t *__restrict__ h8, float *__restrict__ af, float *__restrict__ sf,
 	float *__restrict__ hf) {
 	extern __shared__ float dsm[];
+	__shared__ int nlist;
+	const int rounds = RT > 0 ? RT : rounds_rt;
 	const int SX = DT_X + 2 * rounds, SY = DT_Y + 2 * rounds;
 	float *A = dsm;
 	uint8_t *tag = (uint8_t *)(dsm + (size_t)SX * SY * nch);
+	uint32_t *list = (uint32_t *)(tag + ((SX * SY + 15) & ~15)); // (ly << 16) | lx of the NaN texels
 	const int x0 = (int)(blockIdx.x * DT_X) - rounds, y0 = (int)(blockIdx.y * DT_Y) - rounds;
-	for (int i = threadIdx.x; i < SX * SY; i += blockDim.x) {
-		const int gx = x0 + i % SX, gy = y0 + i / SX;
-		const bool in = gx >= 0 && gy >= 0 && gx < (int)W && gy < (int)H;
-		const float *src = img + ((uint64_t)(in ? gy : 0) * W + (in ? gx : 0)) * nch;
-		for (int c = 0; c < nch; c++) A[i * nch + c] = in ? src[c] : NAN;
-		tag[i] = !in ? DT_ABSENT : (isnan(src[0]) ? DT_NAN : 0);
+	const unsigned lane = threadIdx.x & 31;
+	if (threadIdx.x == 0) nlist = 0;
+	__syncthreads();
+	for (int i0 = 0; i0 < SX * SY; i0 += blockDim.x) { // uniform trip count: the ballot below has every lane
+		const int i = i0 + (int)threadIdx.x;
+		const int lx = i % SX, ly = i / SX;
+		bool empty = false;
+		if (i < SX * SY) {
+			const int gx = x0 + lx, gy = y0 + ly;
+			const bool in = gx >= 0 && gy >= 0 && gx < (int)W && gy < (int)H;
+			const float *src = img + ((uint64_t)(in ? gy : 0) * W + (in ? gx : 0)) * nch;
+			for (int c = 0; c < nch; c++) A[i * nch + c] = in ? src[c] : NAN;
+			const uint8_t t = !in ? DT_ABSENT : (isnan(src[0]) ? DT_NAN : 0);
+			tag[i] = t;
+			empty = t == DT_NAN && lx >= 1 && lx < SX - 1 && ly >= 1 && ly < SY - 1;
+		}
+		const unsigned m = __ballot_sync(0xFFFFFFFFu, empty);
+		int base = 0;
+		if (lane == 0 && m) base = atomicAdd(&nlist, __popc(m));
+		base = __shfl_sync(0xFFFFFFFFu, base, 0);
+		if (empty) list[base + __popc(m & ((1u << lane) - 1u))] = ((uint32_t)ly << 16) | (uint32_t)lx;
 	}
 	__syncthreads();
-	for (int k = 1; k <= rounds; k++) {
-		const int rx = SX - 2 * k, ry = SY - 2 * k;
-		for (int j = threadIdx.x; j < rx * ry; j += blockDim.x) {
-			const int lx = k + j % rx, ly = k + j / rx;
+	const int nl = nlist;
+	for (int k = 1; k <= rounds && nl > 0; k++) {
+		for (int e = threadIdx.x; e < nl; e += blockDim.x) {
+			const int lx = (int)(list[e] & 0xFFFFu), ly = (int)(list[e] >> 16);
+			if (lx < k || lx >= SX - k || ly < k || ly >= SY - k) continue;
 			const int i = ly * SX + lx;
 			if (tag[i] != DT_NAN) continue;
 			float acc[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -285,7 +309,11 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 	up_synth_program P{};
 	if (synth) {
 		P = *synth;
-		tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+		if (spec_of(P) == SPEC_PERLIN_CELL)
+			tex_shade_kernel<true, 2, CELL_EU_SUB><<<blocks_for((const void *)tex_shade_kernel<true, 2, CELL_EU_SUB>, 128, n), 128, 0, s>>>(m, W, H,
+				owner, M, P, purpose, img0, ach);
+		else
+			tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
 	} else {
 		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
 	}
@@ -293,10 +321,12 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 	if (dilation > 0 && dilation <= DT_MAX_ROUNDS) {
 		// every round and the output split in one launch (shared-memory tiles)
 		const size_t smem = dilate_smem(dilation, nch);
-		e = cudaFuncSetAttribute((const void *)tex_dilate_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		const void *kern = dilation == 7 ? (const void *)tex_dilate_fused_kernel<7> : (const void *)tex_dilate_fused_kernel<0>;
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (e != cudaSuccess) return e;
 		const dim3 grid((W + DT_X - 1) / DT_X, (H + DT_Y - 1) / DT_Y);
-		tex_dilate_fused_kernel<<<grid, 256, smem, s>>>(img0, W, H, nch, ach, dilation, a8, s8, h8, af, sf, hf);
+		if (dilation == 7) tex_dilate_fused_kernel<7><<<grid, 256, smem, s>>>(img0, W, H, nch, ach, dilation, a8, s8, h8, af, sf, hf);
+		else tex_dilate_fused_kernel<0><<<grid, 256, smem, s>>>(img0, W, H, nch, ach, dilation, a8, s8, h8, af, sf, hf);
 		L++;
 	} else {
 		float *cur = img0, *nxt = img1;
