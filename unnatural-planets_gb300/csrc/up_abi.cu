@@ -36,7 +36,7 @@ using namespace up;
 
 enum BufSlot {
 	B_IN0, B_OUT0, B_OUT1, B_OUT2, B_GRAD, B_GRID, B_PARTIALS, B_W,
-	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS,
+	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS, B_DC_FB,
 	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
 	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
@@ -239,6 +239,7 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 void contour_geometry(up_context *ctx, int field, ContourRun &c, float *pos, float *nrm, uint32_t *idx) {
 	DcScratch &S = c.S;
 	S.cell_list = (uint32_t *)buf(ctx, B_DC_CLIST, (size_t)c.ncells * 4);
+	S.fb_list = (uint32_t *)buf(ctx, B_DC_FB, (size_t)c.ncells * 4);
 	S.edge_list = (uint32_t *)buf(ctx, B_DC_ELIST, (size_t)c.nedges * 4);
 	S.quad_list = (uint32_t *)buf(ctx, B_DC_QLIST, (size_t)c.nquads * 4);
 	S.edge_t = (float *)buf(ctx, B_DC_ET, (size_t)c.nedges * 4);

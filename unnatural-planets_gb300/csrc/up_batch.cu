@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(128) batch_qef_kernel(const up_synth_program *
 	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ncells; q += gridDim.x * blockDim.x) {
 		const uint32_t c = find_chunk(off, nchunks, q);
 		const BatchChunkDev &ch = chunks[c];
-		dc_qef_item(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
+		dc_qef_item_inline(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
 			pos + 3 * (uint64_t)q, nullptr);
 	}
 }

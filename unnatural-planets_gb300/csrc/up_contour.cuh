@@ -342,14 +342,35 @@ __device__ __forceinline__ bool dc_qef_solve_f32(float a[3][3], const float r[3]
 	return true;
 }
 
+// vertex position of cell p from its cell-local solution vc, and the unit
+// SDF gradient there (the vertex normal)
+template<class E>
+__device__ __forceinline__ void dc_vertex_out(const E &ev, const GridDev &g, uint32_t p, const float vc[3], float *vpos, float *vnrm) {
+	const uint32_t nx = g.n[0], ny = g.n[1];
+	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
+	const V3f vp = v3(dc_coord(g, 0, i) + vc[0] * g.step[0], dc_coord(g, 1, j) + vc[1] * g.step[1], dc_coord(g, 2, k) + vc[2] * g.step[2]);
+	vpos[0] = vp.x;
+	vpos[1] = vp.y;
+	vpos[2] = vp.z;
+	if (vnrm) {
+		const NG s = ev(vp);
+		const float ln = sqrtf(dot(s.g, s.g));
+		const float il = ln > 0.f ? 1.f / ln : 0.f;
+		vnrm[0] = s.g.x * il;
+		vnrm[1] = s.g.y * il;
+		vnrm[2] = s.g.z * il;
+	}
+}
+
 // QEF vertex and normal of one active cell whose origin is grid point p.
 // Pass 1 gathers the Hermite points of the cell's sign edges (cell-local:
 // 0/1 on the two other axes, t along the edge axis) and their mass point;
 // pass 2 accumulates the normal matrix and residual about the mass point in
-// FP32 (no cancellation: the points are centred first). Cells whose
-// truncation decision is within FP32 rounding take the FP64 solver.
+// FP32 (no cancellation: the points are centred first). Returns false,
+// writing nothing, when the truncation decision is within FP32 rounding:
+// the cell then needs the FP64 solver (dc_qef_vertex_fp64, dc_vertex_out).
 template<class E>
-__device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
+__device__ __forceinline__ bool dc_qef_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
 	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t sxy = nx * ny;
@@ -398,23 +419,19 @@ __device__ __forceinline__ void dc_qef_item(const E &ev, const float *__restrict
 		}
 	}
 	float vc[3];
-	if (!dc_qef_solve_f32(A, rv, m, vc)) {
-		double vd[3];
-		dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
-		vc[0] = (float)vd[0]; vc[1] = (float)vd[1]; vc[2] = (float)vd[2];
-	}
-	const V3f vp = v3(dc_coord(g, 0, i) + vc[0] * g.step[0], dc_coord(g, 1, j) + vc[1] * g.step[1], dc_coord(g, 2, k) + vc[2] * g.step[2]);
-	vpos[0] = vp.x;
-	vpos[1] = vp.y;
-	vpos[2] = vp.z;
-	if (vnrm) {
-		const NG s = ev(vp);
-		const float ln = sqrtf(dot(s.g, s.g));
-		const float il = ln > 0.f ? 1.f / ln : 0.f;
-		vnrm[0] = s.g.x * il;
-		vnrm[1] = s.g.y * il;
-		vnrm[2] = s.g.z * il;
-	}
+	if (!dc_qef_solve_f32(A, rv, m, vc)) return false;
+	dc_vertex_out(ev, g, p, vc, vpos, vnrm);
+	return true;
+}
+// the same with the FP64 solver taken in place
+template<class E>
+__device__ __forceinline__ void dc_qef_item_inline(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
+	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
+	if (dc_qef_item(ev, d, g, p, edge_map, edge_t, edge_n, vpos, vnrm)) return;
+	double vd[3];
+	dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
+	const float vc[3] = {(float)vd[0], (float)vd[1], (float)vd[2]};
+	dc_vertex_out(ev, g, p, vc, vpos, vnrm);
 }
 
 // quad of one interior sign edge: six indices into the cell -> vertex map
@@ -441,13 +458,32 @@ __global__ void __launch_bounds__(256) dc_hermite_kernel(const E ev, const float
 		dc_hermite_item(ev, d, g, edge_list[e], edge_t[e], edge_n + 3 * (uint64_t)e);
 }
 
-// QEF vertex and normal of every active cell
+// QEF vertex and normal of every active cell. Cells whose FP32 truncation
+// decision is not certain are appended to fb_list (count in *fb_count) and
+// solved by dc_qef_fp64_kernel: packed into full warps there, the few FP64
+// cells do not hold whole warps of this kernel on the slow FP64 pipe.
 template<class E>
 __global__ void __launch_bounds__(128) dc_qef_kernel(const E ev, const float *__restrict__ d, const GridDev g,
 	const uint32_t *__restrict__ cell_list, uint32_t ncells, const uint32_t *__restrict__ edge_map,
-	const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm) {
+	const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm,
+	uint32_t *__restrict__ fb_list, uint32_t *__restrict__ fb_count) {
 	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x)
-		dc_qef_item(ev, d, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nrm ? nrm + 3 * (uint64_t)c : nullptr);
+		if (!dc_qef_item(ev, d, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nrm ? nrm + 3 * (uint64_t)c : nullptr))
+			fb_list[atomicAdd(fb_count, 1u)] = c;
+}
+template<class E>
+__global__ void __launch_bounds__(128) dc_qef_fp64_kernel(const E ev, const float *__restrict__ d, const GridDev g,
+	const uint32_t *__restrict__ cell_list, const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t,
+	const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm, const uint32_t *__restrict__ fb_list,
+	const uint32_t *__restrict__ fb_count) {
+	const uint32_t n = *fb_count;
+	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+		const uint32_t c = fb_list[e], p = cell_list[c];
+		double vd[3];
+		dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
+		const float vc[3] = {(float)vd[0], (float)vd[1], (float)vd[2]};
+		dc_vertex_out(ev, g, p, vc, pos + 3 * (uint64_t)c, nrm ? nrm + 3 * (uint64_t)c : nullptr);
+	}
 }
 
 cudaError_t dc_quads_launch(const float *d, const GridDev &g, const DcScratch &S, uint32_t nquads, uint32_t *idx, cudaStream_t s);
@@ -464,10 +500,18 @@ cudaError_t dc_geometry_t(const E &ev, const float *d, const GridDev &g, DcScrat
 		if (e != cudaSuccess) return e;
 	}
 	if (ncells) {
+		uint32_t *fb_count = S.totals + 3;
+		cudaError_t e = cudaMemsetAsync(fb_count, 0, sizeof(uint32_t), s);
+		if (e != cudaSuccess) return e;
 		const int b = persistent_blocks((const void *)dc_qef_kernel<E>, 128);
 		const uint32_t need = (ncells + 127) / 128;
-		dc_qef_kernel<E><<<need < (uint32_t)b ? need : (uint32_t)b, 128, 0, s>>>(ev, d, g, S.cell_list, ncells, S.edge_map, S.edge_t, S.edge_n, pos, nrm);
-		cudaError_t e = cudaGetLastError();
+		dc_qef_kernel<E><<<need < (uint32_t)b ? need : (uint32_t)b, 128, 0, s>>>(ev, d, g, S.cell_list, ncells, S.edge_map, S.edge_t, S.edge_n, pos, nrm,
+			S.fb_list, fb_count);
+		// the FP64 cells: as many blocks as the count could need, each exits when past it
+		const int b64 = persistent_blocks((const void *)dc_qef_fp64_kernel<E>, 128);
+		dc_qef_fp64_kernel<E><<<need < (uint32_t)b64 ? need : (uint32_t)b64, 128, 0, s>>>(ev, d, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
+			nrm, S.fb_list, fb_count);
+		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}
 	return dc_quads_launch(d, g, S, nquads, idx, s);

@@ -49,6 +49,7 @@ struct DcScratch {
 	float *edge_t;         // capacity edges
 	float *edge_n;          // 3 * capacity edges
 	uint32_t *signs;        // dc_sign_words(grid): bit-packed d < 0
+	uint32_t *fb_list;      // capacity cells: cells left to the FP64 QEF (count in totals[3])
 };
 uint32_t dc_num_blocks(const GridDev &g);
 uint64_t dc_sign_words(const GridDev &g);
