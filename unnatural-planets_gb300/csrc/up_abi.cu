@@ -36,7 +36,7 @@ using namespace up;
 
 enum BufSlot {
 	B_IN0, B_OUT0, B_OUT1, B_OUT2, B_GRAD, B_GRID, B_PARTIALS, B_W,
-	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS, B_DC_FB,
+	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS, B_DC_FB, B_DC_FBF,
 	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
 	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
@@ -62,6 +62,7 @@ struct up_context {
 	// sampling of slab k + 1 (created on first use)
 	cudaStream_t copy_stream = nullptr;
 	cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr; // contouring: FP64 QEF cells on copy_stream
 };
 
 namespace {
@@ -82,6 +83,19 @@ void check(cudaError_t e, const char *what) {
 	if (e == cudaSuccess) return;
 	if (e == cudaErrorMemoryAllocation) throw Fail{UP_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e)};
 	throw Fail{UP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+// the context's second stream and its events, created on first use: host
+// copies of up_sdf_grid and the FP64 QEF cells of contouring run there
+void side_stream(up_context *ctx) {
+	if (ctx->copy_stream) return;
+	check(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+	for (int b = 0; b < 2; b++) {
+		check(cudaEventCreateWithFlags(&ctx->ev_done[b], cudaEventDisableTiming), "cudaEventCreate");
+		check(cudaEventCreateWithFlags(&ctx->ev_copied[b], cudaEventDisableTiming), "cudaEventCreate");
+	}
+	check(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+	check(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming), "cudaEventCreate");
 }
 
 void *buf(up_context *ctx, int slot, size_t bytes) {
@@ -240,6 +254,11 @@ void contour_geometry(up_context *ctx, int field, ContourRun &c, float *pos, flo
 	DcScratch &S = c.S;
 	S.cell_list = (uint32_t *)buf(ctx, B_DC_CLIST, (size_t)c.ncells * 4);
 	S.fb_list = (uint32_t *)buf(ctx, B_DC_FB, (size_t)c.ncells * 4);
+	S.fb_flag = (uint8_t *)buf(ctx, B_DC_FBF, (size_t)c.ncells);
+	side_stream(ctx);
+	S.side = ctx->copy_stream;
+	S.ev_fork = ctx->ev_fork;
+	S.ev_join = ctx->ev_join;
 	S.edge_list = (uint32_t *)buf(ctx, B_DC_ELIST, (size_t)c.nedges * 4);
 	S.quad_list = (uint32_t *)buf(ctx, B_DC_QLIST, (size_t)c.nquads * 4);
 	S.edge_t = (float *)buf(ctx, B_DC_ET, (size_t)c.nedges * 4);
@@ -257,13 +276,7 @@ void contour_geometry(up_context *ctx, int field, ContourRun &c, float *pos, flo
 constexpr size_t GRID_PIPE_MIN = (size_t)1 << 22; // samples
 constexpr int GRID_PIPE_SLABS = 16;
 int sdf_grid_pipelined(up_context *ctx, uint32_t mask, const GridDev &g, float *const out[3], float *grad) {
-	if (!ctx->copy_stream) {
-		check(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-		for (int b = 0; b < 2; b++) {
-			check(cudaEventCreateWithFlags(&ctx->ev_done[b], cudaEventDisableTiming), "cudaEventCreate");
-			check(cudaEventCreateWithFlags(&ctx->ev_copied[b], cudaEventDisableTiming), "cudaEventCreate");
-		}
-	}
+	side_stream(ctx);
 	const uint32_t nz = g.n[2];
 	const size_t plane = (size_t)g.n[0] * g.n[1];
 	const size_t n = plane * nz;
@@ -416,6 +429,8 @@ int up_context_destroy(up_context *ctx) {
 		if (ctx->ev_done[b]) cudaEventDestroy(ctx->ev_done[b]);
 		if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
 	}
+	if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+	if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
 	delete ctx;
 	return UP_OK;
 }

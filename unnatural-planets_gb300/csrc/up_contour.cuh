@@ -458,18 +458,37 @@ __global__ void __launch_bounds__(256) dc_hermite_kernel(const E ev, const float
 		dc_hermite_item(ev, d, g, edge_list[e], edge_t[e], edge_n + 3 * (uint64_t)e);
 }
 
-// QEF vertex and normal of every active cell. Cells whose FP32 truncation
-// decision is not certain are appended to fb_list (count in *fb_count) and
-// solved by dc_qef_fp64_kernel: packed into full warps there, the few FP64
-// cells do not hold whole warps of this kernel on the slow FP64 pipe.
+// QEF vertex of every active cell (positions only). Cells whose FP32
+// truncation decision is not certain are flagged, appended to fb_list (count
+// in *fb_count) and solved, normal included, by dc_qef_fp64_kernel: packed
+// into full warps there, the few FP64 cells do not hold whole warps of this
+// kernel on the slow FP64 pipe, and their latency overlaps dc_normal_kernel.
 template<class E>
 __global__ void __launch_bounds__(128) dc_qef_kernel(const E ev, const float *__restrict__ d, const GridDev g,
 	const uint32_t *__restrict__ cell_list, uint32_t ncells, const uint32_t *__restrict__ edge_map,
-	const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm,
+	const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, uint8_t *__restrict__ fb_flag,
 	uint32_t *__restrict__ fb_list, uint32_t *__restrict__ fb_count) {
-	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x)
-		if (!dc_qef_item(ev, d, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nrm ? nrm + 3 * (uint64_t)c : nullptr))
-			fb_list[atomicAdd(fb_count, 1u)] = c;
+	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
+		const bool ok = dc_qef_item(ev, d, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nullptr);
+		fb_flag[c] = ok ? 0 : 1;
+		if (!ok) fb_list[atomicAdd(fb_count, 1u)] = c;
+	}
+}
+// unit SDF gradient at the vertex of every cell solved in FP32
+template<class E>
+__global__ void __launch_bounds__(256) dc_normal_kernel(const E ev, const float *__restrict__ pos, const uint8_t *__restrict__ fb_flag,
+	uint32_t ncells, float *__restrict__ nrm) {
+	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
+		if (fb_flag[c]) continue;
+		const float *vp = pos + 3 * (uint64_t)c;
+		const NG s = ev(v3(vp[0], vp[1], vp[2]));
+		const float ln = sqrtf(dot(s.g, s.g));
+		const float il = ln > 0.f ? 1.f / ln : 0.f;
+		float *o = nrm + 3 * (uint64_t)c;
+		o[0] = s.g.x * il;
+		o[1] = s.g.y * il;
+		o[2] = s.g.z * il;
+	}
 }
 template<class E>
 __global__ void __launch_bounds__(128) dc_qef_fp64_kernel(const E ev, const float *__restrict__ d, const GridDev g,
@@ -499,22 +518,36 @@ cudaError_t dc_geometry_t(const E &ev, const float *d, const GridDev &g, DcScrat
 		cudaError_t e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}
-	if (ncells) {
-		uint32_t *fb_count = S.totals + 3;
-		cudaError_t e = cudaMemsetAsync(fb_count, 0, sizeof(uint32_t), s);
-		if (e != cudaSuccess) return e;
-		const int b = persistent_blocks((const void *)dc_qef_kernel<E>, 128);
-		const uint32_t need = (ncells + 127) / 128;
-		dc_qef_kernel<E><<<need < (uint32_t)b ? need : (uint32_t)b, 128, 0, s>>>(ev, d, g, S.cell_list, ncells, S.edge_map, S.edge_t, S.edge_n, pos, nrm,
-			S.fb_list, fb_count);
-		// the FP64 cells: as many blocks as the count could need, each exits when past it
-		const int b64 = persistent_blocks((const void *)dc_qef_fp64_kernel<E>, 128);
-		dc_qef_fp64_kernel<E><<<need < (uint32_t)b64 ? need : (uint32_t)b64, 128, 0, s>>>(ev, d, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
-			nrm, S.fb_list, fb_count);
-		e = cudaGetLastError();
-		if (e != cudaSuccess) return e;
+	if (!ncells) return dc_quads_launch(d, g, S, nquads, idx, s);
+	uint32_t *fb_count = S.totals + 3;
+	cudaError_t e = cudaMemsetAsync(fb_count, 0, sizeof(uint32_t), s);
+	if (e != cudaSuccess) return e;
+	const int b = persistent_blocks((const void *)dc_qef_kernel<E>, 128);
+	const uint32_t need = (ncells + 127) / 128;
+	dc_qef_kernel<E><<<need < (uint32_t)b ? need : (uint32_t)b, 128, 0, s>>>(ev, d, g, S.cell_list, ncells, S.edge_map, S.edge_t, S.edge_n, pos,
+		S.fb_flag, S.fb_list, fb_count);
+	// the FP64 cells (a grid as large as the count could need; blocks past it
+	// exit) on the side stream, beside the normals and quads on s
+	cudaStream_t s64 = s;
+	if (S.side) {
+		if ((e = cudaEventRecord(S.ev_fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(S.side, S.ev_fork, 0)) != cudaSuccess) return e;
+		s64 = S.side;
 	}
-	return dc_quads_launch(d, g, S, nquads, idx, s);
+	const int b64 = persistent_blocks((const void *)dc_qef_fp64_kernel<E>, 128);
+	dc_qef_fp64_kernel<E><<<need < (uint32_t)b64 ? need : (uint32_t)b64, 128, 0, s64>>>(ev, d, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
+		nrm, S.fb_list, fb_count);
+	if (nrm) {
+		const int bn = persistent_blocks((const void *)dc_normal_kernel<E>, 256);
+		const uint32_t needn = (ncells + 255) / 256;
+		dc_normal_kernel<E><<<needn < (uint32_t)bn ? needn : (uint32_t)bn, 256, 0, s>>>(ev, pos, S.fb_flag, ncells, nrm);
+	}
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	e = dc_quads_launch(d, g, S, nquads, idx, s);
+	if (e == cudaSuccess && S.side) {
+		if ((e = cudaEventRecord(S.ev_join, S.side)) != cudaSuccess) return e;
+		e = cudaStreamWaitEvent(s, S.ev_join, 0);
+	}
+	return e;
 }
 
 } // namespace up

@@ -50,6 +50,9 @@ struct DcScratch {
 	float *edge_n;          // 3 * capacity edges
 	uint32_t *signs;        // dc_sign_words(grid): bit-packed d < 0
 	uint32_t *fb_list;      // capacity cells: cells left to the FP64 QEF (count in totals[3])
+	uint8_t *fb_flag;       // capacity cells: 1 = left to the FP64 QEF
+	cudaStream_t side;      // optional: the FP64 QEF runs there (forked and joined with the two events)
+	cudaEvent_t ev_fork, ev_join;
 };
 uint32_t dc_num_blocks(const GridDev &g);
 uint64_t dc_sign_words(const GridDev &g);
