@@ -50,8 +50,8 @@ METRIC = "SDF+grad Gsamples/s at 512^3 (fused value+gradient; plain and ms/plane
 UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
-# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (229.67 MB / 16,777,216)
-TRAFFIC_PER_SAMPLE_FUSED = 229.666816e6 / 16777216
+# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (234.65 MB / 16,777,216)
+TRAFFIC_PER_SAMPLE_FUSED = 234.652160e6 / 16777216
 
 
 def _pkg():
@@ -572,6 +572,29 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def run_only(args) -> None:
+    """one secondary workload alone (for profiling captures): prints its result"""
+    import torch
+    up = _pkg()
+    W = up.workloads
+    stream = torch.cuda.current_stream()
+    if args.only == "atlas":
+        P = W.torus_spheres_ridged_cellular()
+        planet = up.Planet(program=P)
+        planet.set_stream(stream.cuda_stream)
+        pos0, nrm0, idx0 = planet.contour(W.grid(W.GRID_C2, n=(args.grid,) * 3))
+        r = extra_atlas(up, W, planet, stream, pos0, nrm0, idx0)
+    elif args.only == "adjoint":
+        r = extra_adjoint(up, W, stream)
+    elif args.only == "batch":
+        r = extra_batch(up, W, stream)
+    elif args.only == "fit":
+        r = extra_fit(up, W, stream)
+    else:
+        r = extra_modes(up, stream)
+    print(json.dumps({"only": args.only, **r}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -580,8 +603,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", type=int, default=512, help="grid edge (512 is the benchmark; smaller for profiling captures)")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads (atlas, adjoint, batch, fit, modes)")
+    ap.add_argument("--only", choices=["atlas", "adjoint", "batch", "fit", "modes"],
+                    help="run one secondary workload alone and print its result (profiling captures)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.only:
+        run_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
