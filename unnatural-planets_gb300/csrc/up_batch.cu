@@ -9,8 +9,10 @@
 //   sample  persistent blocks pull 1024-sample tiles from a device work
 //           counter; a tile belongs to one chunk (binary search of the tile
 //           table); values go to one concatenated grid
-//   count   per 1024-point block of every chunk: active cells, sign edges,
-//           quads (same rules as up_contour.cuh)
+//   signs   the sign bits of every chunk, 32 points per word (chunk c's
+//           words start at word_off)
+//   count   per 8192-point block of every chunk: active cells, sign edges,
+//           quads from the sign words (dc_word_flags of up_contour.cuh)
 //   scan    exclusive scan of all block counts (global order = chunk order)
 //   offsets per-chunk list offsets from the scan
 //   emit    ordered lists and per-chunk maps
@@ -32,6 +34,7 @@ struct BatchChunkDev {
 	GridDev g;
 	uint32_t planet;
 	uint32_t pt_off, cell_off, blk_off, tile_off;
+	uint32_t word_off, nwords; // sign words: ceil(points / 32) + 2 (zero slack for dc_bits_at)
 	float band; // narrow band of contouring (0: exact values, when the caller reads them)
 };
 
@@ -52,18 +55,31 @@ __device__ __forceinline__ float bgrid_coord(const GridDev &g, int a, uint32_t i
 	return __fadd_rn(__fmul_rn((float)i, g.step[a]), g.lo[a]);
 }
 
+// value of a tile's sample with the planet's layer types fixed at compile
+// time where they are the batch planets' (one Perlin or one simplex layer)
+__device__ __forceinline__ float batch_eval(const up_synth_program &P, V3f p) {
+	if (P.n_layers == 1 && P.layer[0].type == UP_NOISE_PERLIN) return synth_eval<false, 2, -1>(P, p).v;
+	if (P.n_layers == 1 && P.layer[0].type == UP_NOISE_SIMPLEX) return synth_eval<false, 3, -1>(P, p).v;
+	return synth_eval<false, -1, -1>(P, p).v;
+}
+
+// A tile in two passes: every sample's base shape, stored at once where the
+// sample lies outside the narrow band; the others are listed in shared
+// memory and evaluated in full by consecutive threads, so the noise runs in
+// full warps however the band crosses the tile.
 template<int THREADS>
 __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ tile_starts, uint32_t nchunks, uint32_t ntiles, float *__restrict__ d, unsigned *__restrict__ counter,
 	unsigned *__restrict__ nanflag) {
-	__shared__ uint32_t tile;
+	__shared__ uint32_t tile, nnear;
+	__shared__ uint16_t near[BATCH_TILE];
+	const uint32_t lane = threadIdx.x & 31;
 	bool bad = false;
 	for (;;) {
-		if (threadIdx.x == 0) tile = atomicAdd(counter, 1u);
+		if (threadIdx.x == 0) { tile = atomicAdd(counter, 1u); nnear = 0; }
 		__syncthreads();
 		const uint32_t t = tile;
-		__syncthreads();
-		if (t >= ntiles) break;
+		if (t >= ntiles) break; // the same for every thread
 		const uint32_t c = find_chunk(tile_starts, nchunks, t);
 		const BatchChunkDev &ch = chunks[c];
 		const up_synth_program &P = planets[ch.planet];
@@ -71,35 +87,74 @@ __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_pr
 		const uint32_t npts = nx * ny * ch.g.n[2];
 		const uint32_t base = (t - ch.tile_off) * BATCH_TILE;
 		#pragma unroll 1
-		for (uint32_t it = threadIdx.x; it < BATCH_TILE; it += THREADS) {
+		for (uint32_t it = threadIdx.x; it < BATCH_TILE; it += THREADS) { // every thread the same trip count
 			const uint32_t s = base + it;
-			if (s >= npts) break;
+			bool full = false;
+			if (s < npts) {
+				if (ch.band > 0.f) {
+					const uint32_t i = s % nx, r = s / nx, j = r % ny, k = r / ny;
+					const float v = synth_base<false>(P, v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k))).v;
+					if (fabsf(v) > ch.band) d[ch.pt_off + s] = v;
+					else full = true;
+				} else {
+					full = true;
+				}
+			}
+			const unsigned m = __ballot_sync(0xFFFFFFFFu, full);
+			uint32_t slot = 0;
+			if (lane == 0 && m) slot = atomicAdd(&nnear, (uint32_t)__popc(m));
+			slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+			if (full) near[slot + __popc(m & ((1u << lane) - 1u))] = (uint16_t)it;
+		}
+		__syncthreads();
+		const uint32_t nn = nnear;
+		#pragma unroll 1
+		for (uint32_t e = threadIdx.x; e < nn; e += THREADS) {
+			const uint32_t s = base + near[e];
 			const uint32_t i = s % nx, r = s / nx, j = r % ny, k = r / ny;
-			const V3f p = v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k));
-			float v = ch.band > 0.f ? synth_base<false>(P, p).v : 0.f;
-			if (!(ch.band > 0.f && fabsf(v) > ch.band)) v = synth_eval<false, -1, -1>(P, p).v;
+			const float v = batch_eval(P, v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k)));
 			d[ch.pt_off + s] = v;
 			bad |= isnan(v);
 		}
+		__syncthreads(); // the tile's list is read before the next tile is taken
 	}
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
 }
 
-__global__ void __launch_bounds__(DC_T) batch_count_kernel(const float *__restrict__ d, const BatchChunkDev *__restrict__ chunks,
+// sign words of every chunk: a warp packs BATCH_SIGN_U consecutive words
+// (each looked up in the chunk table, usually the chunk of the word before)
+constexpr int BATCH_SIGN_U = 8;
+__global__ void __launch_bounds__(256) batch_signs_kernel(const float *__restrict__ d, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ word_starts, uint32_t nchunks, uint32_t nwords, uint32_t *__restrict__ bits) {
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t step = ((gridDim.x * blockDim.x) >> 5) * BATCH_SIGN_U;
+	uint32_t c = 0;
+	for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * BATCH_SIGN_U; w0 < nwords; w0 += step) { // warp-uniform
+		uint32_t mine = 0;
+		#pragma unroll
+		for (int u = 0; u < BATCH_SIGN_U; u++) {
+			const uint32_t w = w0 + u;
+			if (w >= nwords) break;
+			if (!(w >= word_starts[c] && (c + 1 == nchunks || w < word_starts[c + 1]))) c = find_chunk(word_starts, nchunks, w);
+			const BatchChunkDev &ch = chunks[c];
+			const uint32_t p = 32 * (w - ch.word_off) + lane;
+			const bool in = p < ch.g.n[0] * ch.g.n[1] * ch.g.n[2] && __ldg(d + ch.pt_off + p) < 0.f;
+			const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+			if (lane == (uint32_t)u) mine = m;
+		}
+		if (lane < BATCH_SIGN_U && w0 + lane < nwords) bits[w0 + lane] = mine;
+	}
+}
+
+__global__ void __launch_bounds__(DC_T) batch_count_kernel(const uint32_t *__restrict__ bits, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ blk_starts, uint32_t nchunks, uint32_t nblocks, uint32_t *__restrict__ blk) {
 	const uint32_t c = find_chunk(blk_starts, nchunks, blockIdx.x);
 	const BatchChunkDev &ch = chunks[c];
 	const uint32_t npts = ch.g.n[0] * ch.g.n[1] * ch.g.n[2];
-	const uint32_t base = (blockIdx.x - ch.blk_off) * DC_PB + threadIdx.x * DC_ITEMS;
-	const float *dc = d + ch.pt_off;
-	uint64_t cnt = 0;
-	#pragma unroll
-	for (int it = 0; it < DC_ITEMS; it++) {
-		const uint32_t p = base + it;
-		if (p < npts) cnt += pack_counts(point_flags(dc, ch.g, p));
-	}
+	const uint64_t w = (uint64_t)(blockIdx.x - ch.blk_off) * DC_T + threadIdx.x;
+	const WordFlags f = dc_word_flags(bits + ch.word_off, ch.nwords, ch.g, w, npts);
 	uint64_t tot;
-	block_exscan<DC_T>(cnt, tot);
+	block_exscan<DC_T>(dc_word_counts(f), tot);
 	if (threadIdx.x == 0) {
 		blk[blockIdx.x] = (uint32_t)(tot & 0x1FFFFF);
 		blk[nblocks + blockIdx.x] = (uint32_t)((tot >> 21) & 0x1FFFFF);
@@ -116,52 +171,46 @@ __global__ void batch_offsets_kernel(const BatchChunkDev *__restrict__ chunks, u
 	}
 }
 
-__global__ void __launch_bounds__(DC_T) batch_emit_kernel(const float *__restrict__ d, const BatchChunkDev *__restrict__ chunks,
+__global__ void __launch_bounds__(DC_T) batch_emit_kernel(const uint32_t *__restrict__ bits, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ blk_starts, uint32_t nchunks, uint32_t nblocks, const uint32_t *__restrict__ blk, uint32_t *__restrict__ cell_list,
 	uint32_t *__restrict__ cell_map, uint32_t *__restrict__ edge_list, uint32_t *__restrict__ edge_map, uint32_t *__restrict__ quad_list) {
 	const uint32_t c = find_chunk(blk_starts, nchunks, blockIdx.x);
 	const BatchChunkDev &ch = chunks[c];
 	const GridDev g = ch.g;
 	const uint32_t npts = g.n[0] * g.n[1] * g.n[2];
-	const uint32_t base = (blockIdx.x - ch.blk_off) * DC_PB + threadIdx.x * DC_ITEMS;
-	const float *dc = d + ch.pt_off;
-	PointFlags f[DC_ITEMS];
-	uint64_t cnt = 0;
-	#pragma unroll
-	for (int it = 0; it < DC_ITEMS; it++) {
-		const uint32_t p = base + it;
-		f[it].bits = 0;
-		if (p < npts) f[it] = point_flags(dc, g, p);
-		cnt += pack_counts(f[it]);
-	}
+	const uint64_t w = (uint64_t)(blockIdx.x - ch.blk_off) * DC_T + threadIdx.x;
+	const WordFlags f = dc_word_flags(bits + ch.word_off, ch.nwords, g, w, npts);
 	uint64_t tot;
-	const uint64_t o = block_exscan<DC_T>(cnt, tot);
+	const uint64_t o = block_exscan<DC_T>(dc_word_counts(f), tot);
 	uint32_t co = blk[blockIdx.x] + (uint32_t)(o & 0x1FFFFF);
 	uint32_t eo = blk[nblocks + blockIdx.x] + (uint32_t)((o >> 21) & 0x1FFFFF);
 	uint32_t qo = blk[2 * nblocks + blockIdx.x] + (uint32_t)(o >> 42);
+	const uint32_t p0 = (uint32_t)(32 * w);
 	const uint32_t nx = g.n[0], ny = g.n[1], cx = nx - 1, cy = ny - 1;
 	uint32_t *cmap = cell_map + ch.cell_off;
 	uint32_t *emap = edge_map + 3 * (uint64_t)ch.pt_off;
-	#pragma unroll
-	for (int it = 0; it < DC_ITEMS; it++) {
-		const uint32_t p = base + it;
-		const uint32_t b = f[it].bits;
-		if (!b) continue;
-		if (b & 1u) {
-			const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
-			cell_list[co] = p;
-			cmap[(k * cy + j) * cx + i] = co;
-			co++;
-		}
+	// the same order as the per-point form: cells in point order, then each
+	// point's edges x, y, z (lists stay in ascending point order)
+	for (uint32_t m = f.cell; m; m &= m - 1) {
+		const uint32_t p = p0 + (uint32_t)(__ffs(m) - 1);
+		const uint32_t r = p / nx, i = p - r * nx, j = r % ny, k = r / ny;
+		cell_list[co] = p;
+		cmap[(k * cy + j) * cx + i] = co;
+		co++;
+	}
+	for (uint32_t m = f.ex | f.ey | f.ez; m; m &= m - 1) {
+		const uint32_t b = (uint32_t)(__ffs(m) - 1);
+		const uint32_t p = p0 + b;
+		const uint32_t e[3] = {f.ex, f.ey, f.ez}, q[3] = {f.qx, f.qy, f.qz};
 		#pragma unroll
-		for (int a = 0; a < 3; a++)
-			if (b & (2u << a)) {
-				const uint32_t code = 3 * p + a;
-				edge_list[eo] = code;
-				emap[code] = eo;
-				if (b & (16u << a)) quad_list[qo++] = eo;
-				eo++;
-			}
+		for (int a = 0; a < 3; a++) {
+			if (!((e[a] >> b) & 1u)) continue;
+			const uint32_t code = 3 * p + a;
+			edge_list[eo] = code;
+			emap[code] = eo;
+			if ((q[a] >> b) & 1u) quad_list[qo++] = eo;
+			eo++;
+		}
 	}
 }
 
@@ -182,15 +231,34 @@ __global__ void __launch_bounds__(256) batch_hermite_kernel(const up_synth_progr
 	}
 }
 
+// FP32 QEF of every cell; the cells that need the FP64 solver go to fb_list
+// (count in *fb_count) for batch_qef_fp64_kernel (see dc_qef_kernel)
 __global__ void __launch_bounds__(128) batch_qef_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ cell_list,
-	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos) {
+	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos,
+	uint32_t *__restrict__ fb_list, uint32_t *__restrict__ fb_count) {
 	const uint32_t ncells = off[nchunks];
 	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ncells; q += gridDim.x * blockDim.x) {
 		const uint32_t c = find_chunk(off, nchunks, q);
 		const BatchChunkDev &ch = chunks[c];
-		dc_qef_item_inline(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
-			pos + 3 * (uint64_t)q, nullptr);
+		if (!dc_qef_item(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
+				pos + 3 * (uint64_t)q, nullptr))
+			fb_list[atomicAdd(fb_count, 1u)] = q;
+	}
+}
+__global__ void __launch_bounds__(128) batch_qef_fp64_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
+	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ cell_list,
+	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos,
+	const uint32_t *__restrict__ fb_list, const uint32_t *__restrict__ fb_count) {
+	const uint32_t n = *fb_count;
+	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+		const uint32_t q = fb_list[e];
+		const uint32_t c = find_chunk(off, nchunks, q);
+		const BatchChunkDev &ch = chunks[c];
+		double vd[3];
+		dc_qef_vertex_fp64(d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n, vd);
+		const float vc[3] = {(float)vd[0], (float)vd[1], (float)vd[2]};
+		dc_vertex_out(BatchEvalF{planets + ch.planet}, ch.g, cell_list[q], vc, pos + 3 * (uint64_t)q, nullptr);
 	}
 }
 
@@ -230,7 +298,8 @@ struct BatchState {
 	uint32_t nchunks = 0, npts = 0, ncells_all = 0, nblocks = 0, ntiles = 0;
 	uint32_t ncells = 0, nedges = 0, nquads = 0;
 	int threads = 256;             // autotuned sampling block size
-	DevBuf planets, chunks, tiles, blkst, grid, blk, totals, off, cmap, emap, clist, elist, qlist, et, en, pos, idx, counter, flag;
+	uint32_t nwords = 0;
+	DevBuf planets, chunks, tiles, blkst, wordst, grid, signs, blk, totals, off, cmap, emap, clist, elist, qlist, et, en, pos, idx, counter, flag, fb;
 	cudaStream_t stream = nullptr;
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
@@ -261,7 +330,13 @@ static cudaError_t enqueue_sample(BatchState &S, int threads, cudaStream_t s) {
 static cudaError_t enqueue_front(BatchState &S, cudaStream_t s) {
 	cudaError_t e = enqueue_sample(S, S.threads, s);
 	if (e != cudaSuccess) return e;
-	batch_count_kernel<<<S.nblocks, DC_T, 0, s>>>(S.grid.as<float>(), S.chunks.as<BatchChunkDev>(), S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>());
+	{
+		const uint32_t need = (S.nwords + BATCH_SIGN_U * 8 - 1) / (BATCH_SIGN_U * 8); // 8 warps per block
+		const int pb = persistent_blocks((const void *)batch_signs_kernel, 256);
+		batch_signs_kernel<<<need < (uint32_t)pb ? need : (uint32_t)pb, 256, 0, s>>>(S.grid.as<float>(), S.chunks.as<BatchChunkDev>(),
+			S.wordst.as<uint32_t>(), S.nchunks, S.nwords, S.signs.as<uint32_t>());
+	}
+	batch_count_kernel<<<S.nblocks, DC_T, 0, s>>>(S.signs.as<uint32_t>(), S.chunks.as<BatchChunkDev>(), S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>());
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
 	dc_scan_blocks(S.blk.as<uint32_t>(), S.nblocks, S.totals.as<uint32_t>(), s);
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -272,7 +347,7 @@ static cudaError_t enqueue_front(BatchState &S, cudaStream_t s) {
 static cudaError_t enqueue_back(BatchState &S, cudaStream_t s) {
 	const auto *P = S.planets.as<up_synth_program>();
 	const auto *C = S.chunks.as<BatchChunkDev>();
-	batch_emit_kernel<<<S.nblocks, DC_T, 0, s>>>(S.grid.as<float>(), C, S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>(),
+	batch_emit_kernel<<<S.nblocks, DC_T, 0, s>>>(S.signs.as<uint32_t>(), C, S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>(),
 		S.clist.as<uint32_t>(), S.cmap.as<uint32_t>(), S.elist.as<uint32_t>(), S.emap.as<uint32_t>(), S.qlist.as<uint32_t>());
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
@@ -284,8 +359,13 @@ static cudaError_t enqueue_back(BatchState &S, cudaStream_t s) {
 	batch_hermite_kernel<<<grid_of((const void *)batch_hermite_kernel, 256, S.nedges), 256, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks,
 		S.grid.as<float>(), S.elist.as<uint32_t>(), S.et.as<float>(), S.en.as<float>());
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	uint32_t *fb_count = S.totals.as<uint32_t>() + 3;
+	if ((e = cudaMemsetAsync(fb_count, 0, 4, s)) != cudaSuccess) return e;
 	batch_qef_kernel<<<grid_of((const void *)batch_qef_kernel, 128, S.ncells), 128, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
-		S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<float>(), S.en.as<float>(), S.pos.as<float>());
+		S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<float>(), S.en.as<float>(), S.pos.as<float>(), S.fb.as<uint32_t>(), fb_count);
+	batch_qef_fp64_kernel<<<grid_of((const void *)batch_qef_fp64_kernel, 128, S.ncells), 128, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks,
+		S.grid.as<float>(), S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<float>(), S.en.as<float>(), S.pos.as<float>(), S.fb.as<uint32_t>(),
+		fb_count);
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
 	batch_quads_kernel<<<grid_of((const void *)batch_quads_kernel, 256, S.nquads), 256, 0, s>>>(C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
 		S.qlist.as<uint32_t>(), S.elist.as<uint32_t>(), S.cmap.as<uint32_t>(), S.idx.as<uint32_t>());
@@ -327,8 +407,8 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)) != cudaSuccess) return e;
 		// host chunk table
 		std::vector<BatchChunkDev> tab(nchunks);
-		std::vector<uint32_t> tiles(nchunks), blks(nchunks);
-		uint64_t pts = 0, cells = 0, nb = 0, nt = 0;
+		std::vector<uint32_t> tiles(nchunks), blks(nchunks), words(nchunks);
+		uint64_t pts = 0, cells = 0, nb = 0, nt = 0, nw = 0;
 		for (size_t c = 0; c < nchunks; c++) {
 			BatchChunkDev &t = tab[c];
 			t.g = make_grid(chunks[c].grid);
@@ -339,19 +419,26 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 			t.cell_off = (uint32_t)cells;
 			t.blk_off = (uint32_t)nb;
 			t.tile_off = (uint32_t)nt;
+			t.word_off = (uint32_t)nw;
+			t.nwords = (uint32_t)((n + 31) / 32 + 2);
 			tiles[c] = t.tile_off;
 			blks[c] = t.blk_off;
+			words[c] = t.word_off;
 			pts += n;
 			cells += (uint64_t)(t.g.n[0] - 1) * (t.g.n[1] - 1) * (t.g.n[2] - 1);
-			nb += (n + DC_PB - 1) / DC_PB;
+			nb += (n + DC_WPB - 1) / DC_WPB;
 			nt += (n + BATCH_TILE - 1) / BATCH_TILE;
+			nw += t.nwords;
 		}
 		if (3 * pts >= (1ull << 32)) return cudaErrorInvalidValue;
 		S->nchunks = (uint32_t)nchunks; S->npts = (uint32_t)pts; S->ncells_all = (uint32_t)cells; S->nblocks = (uint32_t)nb; S->ntiles = (uint32_t)nt;
+		S->nwords = (uint32_t)nw;
 		if ((e = S->planets.ensure(nplanets * sizeof(up_synth_program))) != cudaSuccess) return e;
 		if ((e = S->chunks.ensure(nchunks * sizeof(BatchChunkDev))) != cudaSuccess) return e;
 		if ((e = S->tiles.ensure(nchunks * 4)) != cudaSuccess) return e;
 		if ((e = S->blkst.ensure(nchunks * 4)) != cudaSuccess) return e;
+		if ((e = S->wordst.ensure(nchunks * 4)) != cudaSuccess) return e;
+		if ((e = S->signs.ensure(nw * 4)) != cudaSuccess) return e;
 		if ((e = S->grid.ensure(pts * 4)) != cudaSuccess) return e;
 		if ((e = S->blk.ensure(dc_scan_words((uint32_t)nb) * 4)) != cudaSuccess) return e;
 		if ((e = S->totals.ensure(16)) != cudaSuccess) return e;
@@ -370,6 +457,7 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		cudaMemcpyAsync(S->chunks.p, tab.data(), nchunks * sizeof(BatchChunkDev), cudaMemcpyHostToDevice, s);
 		cudaMemcpyAsync(S->tiles.p, tiles.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
 		cudaMemcpyAsync(S->blkst.p, blks.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
+		cudaMemcpyAsync(S->wordst.p, words.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
 		cudaMemsetAsync(S->flag.p, 0, 4, s);
 		// autotune the sampling block size (each candidate runs the full sampling stage once)
 		{
@@ -401,6 +489,7 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = S->et.ensure((size_t)S->nedges * 4)) != cudaSuccess) return e;
 		if ((e = S->en.ensure((size_t)S->nedges * 12)) != cudaSuccess) return e;
 		if ((e = S->pos.ensure((size_t)S->ncells * 12)) != cudaSuccess) return e;
+		if ((e = S->fb.ensure((size_t)S->ncells * 4)) != cudaSuccess) return e;
 		if ((e = S->idx.ensure((size_t)S->nquads * 24)) != cudaSuccess) return e;
 		if ((e = enqueue_back(*S, s)) != cudaSuccess) return e;
 		if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;

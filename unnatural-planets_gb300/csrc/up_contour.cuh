@@ -16,7 +16,7 @@
 // count (per word: active cells, sign edges, quads; dc_word_flags) ->
 // exclusive scan of block counts -> emit (ordered lists and dense maps; order
 // fixed by the scan, no atomics) -> Hermite per edge -> QEF per cell -> quads.
-// Batches of chunks classify per point (point_flags, up_batch.cu).
+// Batches of chunks run the same word kernels per chunk (up_batch.cu).
 #pragma once
 #include "up_internal.h"
 #include "up_noise.cuh"
@@ -29,39 +29,17 @@ __device__ __forceinline__ float dc_coord(const GridDev &g, int a, uint32_t i) {
 	return __fadd_rn(__fmul_rn((float)i, g.step[a]), g.lo[a]);
 }
 
-// per-point flags packed as cells | edges << 21 | quads << 42 (counts per
-// point: cells <= 1, edges <= 3, quads <= 3), plus the per-axis bits
-struct PointFlags { uint32_t bits; }; // bit0 cell, bit1..3 edge x/y/z, bit4..6 quad x/y/z
-
-__device__ __forceinline__ PointFlags point_flags(const float *__restrict__ d, const GridDev &g, uint32_t p) {
-	PointFlags f{0};
-	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
-	const uint32_t i = p % nx, r = p / nx, j = r % ny, k = r / ny;
-	const uint32_t sxy = nx * ny;
-	const bool in0 = __ldg(d + p) < 0.f;
-	const bool hx = i + 1 < nx, hy = j + 1 < ny, hz = k + 1 < nz;
-	const bool inx = hx && (__ldg(d + p + 1) < 0.f);
-	const bool iny = hy && (__ldg(d + p + nx) < 0.f);
-	const bool inz = hz && (__ldg(d + p + sxy) < 0.f);
-	const bool iix = i >= 1 && i + 1 < nx, ijy = j >= 1 && j + 1 < ny, ikz = k >= 1 && k + 1 < nz;
-	if (hx && inx != in0) { f.bits |= 2u; if (ijy && ikz) f.bits |= 16u; }
-	if (hy && iny != in0) { f.bits |= 4u; if (iix && ikz) f.bits |= 32u; }
-	if (hz && inz != in0) { f.bits |= 8u; if (iix && ijy) f.bits |= 64u; }
-	if (hx && hy && hz) {
-		const uint32_t m = (uint32_t)in0 | ((uint32_t)inx << 1) | ((uint32_t)iny << 2) | ((uint32_t)(__ldg(d + p + nx + 1) < 0.f) << 3) |
-			((uint32_t)inz << 4) | ((uint32_t)(__ldg(d + p + sxy + 1) < 0.f) << 5) | ((uint32_t)(__ldg(d + p + sxy + nx) < 0.f) << 6) |
-			((uint32_t)(__ldg(d + p + sxy + nx + 1) < 0.f) << 7);
-		if (m != 0u && m != 255u) f.bits |= 1u;
-	}
-	return f;
-}
-// ---- word-parallel classification (single grids)
+// ---- word-parallel classification
 // The signs (d < 0) of 32 consecutive points form one word (bit b = point
 // 32 w + b; 0 past the grid; two words of zero padding). One thread
 // classifies a word: the neighbour signs along +x, +y, +z are the same
 // bitfield read at offsets 1, nx, nx * ny (funnel shifts of two words), so
 // sign-change edges, quads and active cells are bitwise expressions, gated
-// by per-word masks of the grid boundary conditions of point_flags.
+// by per-word masks of the grid boundary: point (i, j, k) has an edge along
+// x when i + 1 < nx (likewise y, z); that edge emits a quad when the other
+// two indices are interior (1 <= j < ny - 1, 1 <= k < nz - 1); the point is
+// an active cell when i + 1 < nx, j + 1 < ny, k + 1 < nz and the cell's
+// eight corners do not all share one sign.
 constexpr uint32_t DC_WPB = DC_T * 32; // points per block of the word kernels
 
 __device__ __forceinline__ uint32_t dc_bits_at(const uint32_t *__restrict__ B, uint64_t q, uint64_t nalloc) {
@@ -118,12 +96,6 @@ __device__ __forceinline__ uint64_t dc_word_counts(const WordFlags &f) {
 		((uint64_t)(__popc(f.qx) + __popc(f.qy) + __popc(f.qz)) << 42);
 }
 
-__device__ __forceinline__ uint64_t pack_counts(PointFlags f) {
-	const uint64_t c = f.bits & 1u;
-	const uint64_t e = __popc(f.bits & 14u);
-	const uint64_t q = __popc(f.bits & 112u);
-	return c | (e << 21) | (q << 42);
-}
 
 // block-wide exclusive scan of one 64-bit value per thread
 template<int T>
@@ -422,16 +394,6 @@ __device__ __forceinline__ bool dc_qef_item(const E &ev, const float *__restrict
 	if (!dc_qef_solve_f32(A, rv, m, vc)) return false;
 	dc_vertex_out(ev, g, p, vc, vpos, vnrm);
 	return true;
-}
-// the same with the FP64 solver taken in place
-template<class E>
-__device__ __forceinline__ void dc_qef_item_inline(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
-	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
-	if (dc_qef_item(ev, d, g, p, edge_map, edge_t, edge_n, vpos, vnrm)) return;
-	double vd[3];
-	dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
-	const float vc[3] = {(float)vd[0], (float)vd[1], (float)vd[2]};
-	dc_vertex_out(ev, g, p, vc, vpos, vnrm);
 }
 
 // quad of one interior sign edge: six indices into the cell -> vertex map
