@@ -8,9 +8,9 @@
 // Stages (each one launch covering every chunk):
 //   sample  persistent blocks pull 1024-sample tiles from a device work
 //           counter; a tile belongs to one chunk (binary search of the tile
-//           table); values go to one concatenated grid
-//   signs   the sign bits of every chunk, 32 points per word (chunk c's
-//           words start at word_off)
+//           table); values go to one concatenated grid, and the sign bits
+//           of every chunk, 32 points per word, to chunk c's words from
+//           word_off
 //   count   per 8192-point block of every chunk: active cells, sign edges,
 //           quads from the sign words (dc_word_flags of up_contour.cuh)
 //   scan    exclusive scan of all block counts (global order = chunk order)
@@ -36,6 +36,7 @@ struct BatchChunkDev {
 	uint32_t pt_off, cell_off, blk_off, tile_off;
 	uint32_t word_off, nwords; // sign words: ceil(points / 32) + 2 (zero slack for dc_bits_at)
 	float band; // narrow band of contouring (0: exact values, when the caller reads them)
+	FastDiv divx, divy; // by n[0] and n[1]
 };
 
 constexpr uint32_t BATCH_TILE = 1024;
@@ -67,12 +68,15 @@ __device__ __forceinline__ float batch_eval(const up_synth_program &P, V3f p) {
 // sample lies outside the narrow band; the others are listed in shared
 // memory and evaluated in full by consecutive threads, so the noise runs in
 // full warps however the band crosses the tile.
+// The tile's sign words (d < 0, 32 samples a word: a warp's samples in the
+// first pass) are formed in shared memory and stored with the values.
 template<int THREADS>
 __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
-	const uint32_t *__restrict__ tile_starts, uint32_t nchunks, uint32_t ntiles, float *__restrict__ d, unsigned *__restrict__ counter,
-	unsigned *__restrict__ nanflag) {
+	const uint32_t *__restrict__ tile_starts, uint32_t nchunks, uint32_t ntiles, float *__restrict__ d, uint32_t *__restrict__ bits,
+	unsigned *__restrict__ counter, unsigned *__restrict__ nanflag) {
 	__shared__ uint32_t tile, nnear;
 	__shared__ uint16_t near[BATCH_TILE];
+	__shared__ uint32_t words[BATCH_TILE / 32];
 	const uint32_t lane = threadIdx.x & 31;
 	bool bad = false;
 	for (;;) {
@@ -86,16 +90,21 @@ __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_pr
 		const uint32_t nx = ch.g.n[0], ny = ch.g.n[1];
 		const uint32_t npts = nx * ny * ch.g.n[2];
 		const uint32_t base = (t - ch.tile_off) * BATCH_TILE;
+		const FastDiv dx = ch.divx, dy = ch.divy;
 		#pragma unroll 1
 		for (uint32_t it = threadIdx.x; it < BATCH_TILE; it += THREADS) { // every thread the same trip count
 			const uint32_t s = base + it;
-			bool full = false;
+			bool full = false, neg = false;
 			if (s < npts) {
 				if (ch.band > 0.f) {
-					const uint32_t i = s % nx, r = s / nx, j = r % ny, k = r / ny;
+					const uint32_t r = dx.div(s), i = s - r * nx, k = dy.div(r), j = r - k * ny;
 					const float v = synth_base<false>(P, v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k))).v;
-					if (fabsf(v) > ch.band) d[ch.pt_off + s] = v;
-					else full = true;
+					if (fabsf(v) > ch.band) {
+						d[ch.pt_off + s] = v;
+						neg = v < 0.f;
+					} else {
+						full = true;
+					}
 				} else {
 					full = true;
 				}
@@ -105,45 +114,33 @@ __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_pr
 			if (lane == 0 && m) slot = atomicAdd(&nnear, (uint32_t)__popc(m));
 			slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
 			if (full) near[slot + __popc(m & ((1u << lane) - 1u))] = (uint16_t)it;
+			// signs of the stored samples now; the listed ones are or-ed in below
+			const unsigned negs = __ballot_sync(0xFFFFFFFFu, neg);
+			if (lane == 0) words[it >> 5] = negs;
 		}
 		__syncthreads();
 		const uint32_t nn = nnear;
 		#pragma unroll 1
 		for (uint32_t e = threadIdx.x; e < nn; e += THREADS) {
-			const uint32_t s = base + near[e];
-			const uint32_t i = s % nx, r = s / nx, j = r % ny, k = r / ny;
+			const uint32_t it = near[e], s = base + it;
+			const uint32_t r = dx.div(s), i = s - r * nx, k = dy.div(r), j = r - k * ny;
 			const float v = batch_eval(P, v3(bgrid_coord(ch.g, 0, i), bgrid_coord(ch.g, 1, j), bgrid_coord(ch.g, 2, k)));
 			d[ch.pt_off + s] = v;
 			bad |= isnan(v);
+			if (v < 0.f) atomicOr(&words[it >> 5], 1u << (it & 31));
 		}
-		__syncthreads(); // the tile's list is read before the next tile is taken
+		__syncthreads();
+		// the tile's words that belong to the chunk (its data words, and the
+		// two zero words after them from its last tile)
+		const uint32_t w0 = base >> 5;
+		if (threadIdx.x < BATCH_TILE / 32 && w0 + threadIdx.x < ch.nwords) bits[ch.word_off + w0 + threadIdx.x] = words[threadIdx.x];
+		if (threadIdx.x < 2 && base + BATCH_TILE >= npts) {
+			const uint32_t ws = (npts + 31) / 32 + threadIdx.x; // slack words
+			if (ws >= w0 + BATCH_TILE / 32) bits[ch.word_off + ws] = 0u;
+		}
+		__syncthreads(); // the tile's list and words are read before the next tile is taken
 	}
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
-}
-
-// sign words of every chunk: a warp packs BATCH_SIGN_U consecutive words
-// (each looked up in the chunk table, usually the chunk of the word before)
-constexpr int BATCH_SIGN_U = 8;
-__global__ void __launch_bounds__(256) batch_signs_kernel(const float *__restrict__ d, const BatchChunkDev *__restrict__ chunks,
-	const uint32_t *__restrict__ word_starts, uint32_t nchunks, uint32_t nwords, uint32_t *__restrict__ bits) {
-	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t step = ((gridDim.x * blockDim.x) >> 5) * BATCH_SIGN_U;
-	uint32_t c = 0;
-	for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * BATCH_SIGN_U; w0 < nwords; w0 += step) { // warp-uniform
-		uint32_t mine = 0;
-		#pragma unroll
-		for (int u = 0; u < BATCH_SIGN_U; u++) {
-			const uint32_t w = w0 + u;
-			if (w >= nwords) break;
-			if (!(w >= word_starts[c] && (c + 1 == nchunks || w < word_starts[c + 1]))) c = find_chunk(word_starts, nchunks, w);
-			const BatchChunkDev &ch = chunks[c];
-			const uint32_t p = 32 * (w - ch.word_off) + lane;
-			const bool in = p < ch.g.n[0] * ch.g.n[1] * ch.g.n[2] && __ldg(d + ch.pt_off + p) < 0.f;
-			const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
-			if (lane == (uint32_t)u) mine = m;
-		}
-		if (lane < BATCH_SIGN_U && w0 + lane < nwords) bits[w0 + lane] = mine;
-	}
 }
 
 __global__ void __launch_bounds__(DC_T) batch_count_kernel(const uint32_t *__restrict__ bits, const BatchChunkDev *__restrict__ chunks,
@@ -299,7 +296,7 @@ struct BatchState {
 	uint32_t ncells = 0, nedges = 0, nquads = 0;
 	int threads = 256;             // autotuned sampling block size
 	uint32_t nwords = 0;
-	DevBuf planets, chunks, tiles, blkst, wordst, grid, signs, blk, totals, off, cmap, emap, clist, elist, qlist, et, en, pos, idx, counter, flag, fb;
+	DevBuf planets, chunks, tiles, blkst, grid, signs, blk, totals, off, cmap, emap, clist, elist, qlist, et, en, pos, idx, counter, flag, fb;
 	cudaStream_t stream = nullptr;
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
@@ -321,21 +318,16 @@ static cudaError_t enqueue_sample(BatchState &S, int threads, cudaStream_t s) {
 	const int b = sample_blocks(threads);
 	const auto *P = S.planets.as<up_synth_program>();
 	const auto *C = S.chunks.as<BatchChunkDev>();
-	if (threads == 128) batch_sample_kernel<128><<<b, 128, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), S.counter.as<unsigned>(), S.flag.as<unsigned>());
-	else if (threads == 512) batch_sample_kernel<512><<<b, 512, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), S.counter.as<unsigned>(), S.flag.as<unsigned>());
-	else batch_sample_kernel<256><<<b, 256, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	uint32_t *B = S.signs.as<uint32_t>();
+	if (threads == 128) batch_sample_kernel<128><<<b, 128, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	else if (threads == 512) batch_sample_kernel<512><<<b, 512, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	else batch_sample_kernel<256><<<b, 256, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
 	return cudaGetLastError();
 }
 
 static cudaError_t enqueue_front(BatchState &S, cudaStream_t s) {
 	cudaError_t e = enqueue_sample(S, S.threads, s);
 	if (e != cudaSuccess) return e;
-	{
-		const uint32_t need = (S.nwords + BATCH_SIGN_U * 8 - 1) / (BATCH_SIGN_U * 8); // 8 warps per block
-		const int pb = persistent_blocks((const void *)batch_signs_kernel, 256);
-		batch_signs_kernel<<<need < (uint32_t)pb ? need : (uint32_t)pb, 256, 0, s>>>(S.grid.as<float>(), S.chunks.as<BatchChunkDev>(),
-			S.wordst.as<uint32_t>(), S.nchunks, S.nwords, S.signs.as<uint32_t>());
-	}
 	batch_count_kernel<<<S.nblocks, DC_T, 0, s>>>(S.signs.as<uint32_t>(), S.chunks.as<BatchChunkDev>(), S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>());
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
 	dc_scan_blocks(S.blk.as<uint32_t>(), S.nblocks, S.totals.as<uint32_t>(), s);
@@ -407,13 +399,15 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)) != cudaSuccess) return e;
 		// host chunk table
 		std::vector<BatchChunkDev> tab(nchunks);
-		std::vector<uint32_t> tiles(nchunks), blks(nchunks), words(nchunks);
+		std::vector<uint32_t> tiles(nchunks), blks(nchunks);
 		uint64_t pts = 0, cells = 0, nb = 0, nt = 0, nw = 0;
 		for (size_t c = 0; c < nchunks; c++) {
 			BatchChunkDev &t = tab[c];
 			t.g = make_grid(chunks[c].grid);
 			t.planet = chunks[c].planet;
 			t.band = exact_values ? 0.f : contour_band(planets[t.planet], t.g);
+			t.divx = FastDiv::of(t.g.n[0]);
+			t.divy = FastDiv::of(t.g.n[1]);
 			const uint64_t n = (uint64_t)t.g.n[0] * t.g.n[1] * t.g.n[2];
 			t.pt_off = (uint32_t)pts;
 			t.cell_off = (uint32_t)cells;
@@ -423,7 +417,6 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 			t.nwords = (uint32_t)((n + 31) / 32 + 2);
 			tiles[c] = t.tile_off;
 			blks[c] = t.blk_off;
-			words[c] = t.word_off;
 			pts += n;
 			cells += (uint64_t)(t.g.n[0] - 1) * (t.g.n[1] - 1) * (t.g.n[2] - 1);
 			nb += (n + DC_WPB - 1) / DC_WPB;
@@ -437,7 +430,6 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = S->chunks.ensure(nchunks * sizeof(BatchChunkDev))) != cudaSuccess) return e;
 		if ((e = S->tiles.ensure(nchunks * 4)) != cudaSuccess) return e;
 		if ((e = S->blkst.ensure(nchunks * 4)) != cudaSuccess) return e;
-		if ((e = S->wordst.ensure(nchunks * 4)) != cudaSuccess) return e;
 		if ((e = S->signs.ensure(nw * 4)) != cudaSuccess) return e;
 		if ((e = S->grid.ensure(pts * 4)) != cudaSuccess) return e;
 		if ((e = S->blk.ensure(dc_scan_words((uint32_t)nb) * 4)) != cudaSuccess) return e;
@@ -457,15 +449,17 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		cudaMemcpyAsync(S->chunks.p, tab.data(), nchunks * sizeof(BatchChunkDev), cudaMemcpyHostToDevice, s);
 		cudaMemcpyAsync(S->tiles.p, tiles.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
 		cudaMemcpyAsync(S->blkst.p, blks.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
-		cudaMemcpyAsync(S->wordst.p, words.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
 		cudaMemsetAsync(S->flag.p, 0, 4, s);
-		// autotune the sampling block size (each candidate runs the full sampling stage once)
+		// autotune the sampling block size (each candidate runs the full
+		// sampling stage once, after one untimed run that warms the caches)
 		{
 			cudaEvent_t a, b;
 			cudaEventCreate(&a);
 			cudaEventCreate(&b);
 			float best = 1e30f;
+			e = enqueue_sample(*S, 256, s);
 			for (int t : {128, 256, 512}) {
+				if (e != cudaSuccess) break;
 				cudaEventRecord(a, s);
 				if ((e = enqueue_sample(*S, t, s)) != cudaSuccess) break;
 				cudaEventRecord(b, s);
