@@ -6,7 +6,7 @@
 // CPU tasks (tasksRunBlocking, sources/generator.cpp:159,215).
 //
 // Stages (each one launch covering every chunk):
-//   sample  persistent blocks pull 1024-sample tiles from a device work
+//   sample  persistent blocks pull 4096-sample tiles from a device work
 //           counter; a tile belongs to one chunk (binary search of the tile
 //           table); values go to one concatenated grid, and the sign bits
 //           of every chunk, 32 points per word, to chunk c's words from
@@ -39,7 +39,7 @@ struct BatchChunkDev {
 	FastDiv divx, divy; // by n[0] and n[1]
 };
 
-constexpr uint32_t BATCH_TILE = 1024;
+constexpr uint32_t BATCH_TILE = 4096; // timed against 1024 to 16384 samples
 
 __device__ __forceinline__ uint32_t find_chunk(const uint32_t *__restrict__ starts, uint32_t n, uint32_t x) {
 	// last c with starts[c] <= x (starts ascending, starts[0] = 0)
