@@ -288,9 +288,7 @@ def extra_fit(up, W, stream, steps=300):
     n = 32 << 20
     x = _shell(target, n, 0.05, seed=21)
     gg = W.grid(W.GRID_C2, n=(256, 256, 256))
-    ax = [torch.linspace(float(gg.lo[a]), float(gg.hi[a]), 256, device="cuda") for a in range(3)]
-    zz, yy, xx = torch.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
-    xg = torch.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], dim=1).contiguous()
+    xg = AG.grid_positions(gg)  # the grid kernel's sample positions
     d_star = target.sdf_points(x, d=torch.empty(n, device="cuda"))
     s_star = torch.sign(target.sdf_points(xg, d=torch.empty(xg.shape[0], device="cuda")))
     theta = torch.tensor(t0, device="cuda", requires_grad=True)
@@ -301,7 +299,7 @@ def extra_fit(up, W, stream, steps=300):
 
     def step():
         opt.zero_grad()
-        loss = ((AG.sdf(theta, x, planet) - d_star) ** 2).mean() + torch.relu(-AG.sdf(theta, xg, planet) * s_star).mean()
+        loss = ((AG.sdf(theta, x, planet) - d_star) ** 2).mean() + torch.relu(-AG.sdf_grid(theta, gg, planet, xg) * s_star).mean()
         loss.backward()
         opt.step()
         return loss
@@ -335,7 +333,7 @@ def extra_fit(up, W, stream, steps=300):
             "sdf_rms_vs_fp64_oracle": float(np.sqrt(np.mean((fit - ref) ** 2))),
             "what": "torus + 8 spheres - ridged perlin + cellular, 25 parameters; theta* = theta (1 + 0.05 U) seed 1, "
                     "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell + "
-                    "mean(relu(-d sign(d*))) on 256^3; Adam lr 1e-2; SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
+                    "mean(relu(-d sign(d*))) on 256^3 (forward through the grid kernel); Adam lr 1e-2; SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
 
 
 def extra_modes(up, stream):

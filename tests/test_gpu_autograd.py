@@ -74,3 +74,30 @@ def test_gradcheck_4096_points(cuda, up):
         return (d.double() ** 2).mean()
 
     assert torch.autograd.gradcheck(loss, (theta,), eps=2e-3, atol=2e-5, rtol=2e-2, nondet_tol=1e-6, fast_mode=False)
+
+
+def test_grid_function_matches_points(cuda, up, O):
+    """SynthSDFGrid (forward through the grid kernel) against SynthSDF at the
+    same sample positions: grid_positions are the kernels' coordinates (the
+    oracle's grid positions bit for bit), the values agree to FP32
+    reassociation, and the parameter gradients of a hinge loss (most weights
+    zero, skipped by the adjoint) agree with the points form."""
+    torch = cuda
+    AG = importlib.import_module("unnatural-planets_gb300.autograd")
+    W = workloads()
+    P = W.torus_spheres_ridged_cellular()
+    planet = up.Planet(program=P)
+    g = W.grid(W.GRID_C2, n=(40, 37, 33))
+    pos = AG.grid_positions(g)
+    assert np.array_equal(pos.cpu().numpy(), O.grid_positions(g))
+    theta = torch.from_numpy(W.theta_of(P)).cuda()
+    sign = torch.sign(AG.sdf(theta, pos, planet)).detach()
+    t1 = (theta * 1.03).requires_grad_(True)
+    t2 = (theta * 1.03).requires_grad_(True)
+    dg = AG.sdf_grid(t1, g, planet, pos)
+    dp = AG.sdf(t2, pos, planet)
+    assert torch.abs(dg - dp).max().item() < 2e-6
+    torch.relu(-dg * sign).mean().backward()
+    torch.relu(-dp * sign).mean().backward()
+    assert (dg * sign < 0).any() and (dg * sign >= 0).float().mean().item() > 0.5  # a hinge with zero and non-zero weights
+    np.testing.assert_allclose(t1.grad.cpu().numpy(), t2.grad.cpu().numpy(), rtol=1e-4, atol=1e-7)

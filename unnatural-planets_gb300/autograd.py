@@ -1,7 +1,8 @@
 """torch.autograd.Function over the C-ABI SDF of a synthetic planet.
 
 SynthSDF.apply(theta, points, planet) returns d(points; theta) (FP32, on
-the points' device). Its backward calls the library's hand-written adjoint
+the points' device); SynthSDFGrid does the same for every sample of a grid
+through the grid kernel. Its backward calls the library's hand-written adjoint
 (up_sdf_param_backward: octaves recomputed, block partial sums reduced in a
 fixed order) for dL/dtheta and the analytic gradient for dL/dpoints. The
 forward sets the context's parameter vector from theta, so one Planet serves
@@ -36,6 +37,45 @@ class SynthSDF(torch.autograd.Function):
         return dth.to(ctx.theta_dtype), dpts, None
 
 
+class SynthSDFGrid(torch.autograd.Function):
+    """d on every sample of a grid (x fastest, grid.count values) from the
+    x-coherent grid kernel (up_sdf_grid). Its backward is SynthSDF's at the
+    grid's sample positions (grid_positions: the kernels' coordinates)."""
+    @staticmethod
+    def forward(ctx, theta: torch.Tensor, grid, planet, positions: torch.Tensor):
+        th = theta.detach().to(torch.float32).contiguous().cpu()
+        planet.set_theta(th.numpy())
+        d = torch.empty(grid.count, dtype=torch.float32, device=positions.device)
+        planet.sdf_grid(grid, 1, outs=[d, None, None])
+        ctx.planet = planet
+        ctx.save_for_backward(positions)
+        ctx.theta_dtype = theta.dtype
+        return d
+
+    @staticmethod
+    def backward(ctx, dL_dd: torch.Tensor):
+        (pts,) = ctx.saved_tensors
+        w = dL_dd.detach().to(torch.float32).contiguous()
+        dth = torch.empty(len(_theta_of(ctx.planet)), dtype=torch.float32, device=pts.device)
+        ctx.planet.param_backward(pts, w, dtheta=dth)
+        return dth.to(ctx.theta_dtype), None, None, None
+
+
+def grid_positions(grid, device="cuda") -> torch.Tensor:
+    """(count, 3) FP32 sample positions of a grid, x fastest, computed as the
+    kernels compute them: step = (hi - lo) / (n - 1), x_i = i * step + lo
+    (a rounded product, then a rounded sum)."""
+    ax = []
+    for a in range(3):
+        lo = torch.tensor(float(grid.lo[a]), dtype=torch.float32, device=device)
+        hi = torch.tensor(float(grid.hi[a]), dtype=torch.float32, device=device)
+        step = (hi - lo) / torch.tensor(float(int(grid.n[a]) - 1), dtype=torch.float32, device=device)
+        i = torch.arange(int(grid.n[a]), dtype=torch.float32, device=device)
+        ax.append((i * step) + lo)
+    zz, yy, xx = torch.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return torch.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], dim=1).contiguous()
+
+
 def _theta_of(planet):
     from .workloads import theta_of
     return theta_of(planet.program)
@@ -43,3 +83,10 @@ def _theta_of(planet):
 
 def sdf(theta, points, planet):
     return SynthSDF.apply(theta, points, planet)
+
+
+def sdf_grid(theta, grid, planet, positions=None):
+    """d on the grid's samples (flat, x fastest); positions: grid_positions(grid), reused across calls"""
+    if positions is None:
+        positions = grid_positions(grid)
+    return SynthSDFGrid.apply(theta, grid, planet, positions)

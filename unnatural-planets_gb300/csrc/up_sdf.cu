@@ -259,8 +259,12 @@ __global__ void __launch_bounds__(BWD_THREADS) synth_bwd_kernel(const up_synth_p
 	#pragma unroll
 	for (int i = 0; i < ACC_N; i++) acc[i] = 0.f;
 	for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (uint64_t)gridDim.x * blockDim.x) {
+		// a point of weight 0 adds w * dd/dtheta = 0 (the derivatives are
+		// finite for finite parameters): a hinge loss leaves most weights 0
+		const float wi = w[idx];
+		if (wi == 0.f) continue;
 		const V3f p = v3(xyz[3 * idx], xyz[3 * idx + 1], xyz[3 * idx + 2]);
-		synth_bwd<T0, T1>(P, p, w[idx], acc);
+		synth_bwd<T0, T1>(P, p, wi, acc);
 	}
 	// warp sums, then warps in a fixed order: deterministic per block
 	__shared__ float red[BWD_THREADS / 32][ACC_N];
