@@ -69,59 +69,91 @@ __global__ void __launch_bounds__(256) tex_raster_kernel(const TexMesh m, uint32
 	}
 }
 
-// per texel: interpolate position and normal of the owning triangle, color
+// per texel: interpolate position and normal of the owning triangle, color.
+// A block takes tiles of TS_TILE consecutive texels in two passes: the
+// uncovered texels are written NaN at once and the covered ones listed in
+// shared memory, then shaded by consecutive threads, so the coloring runs
+// in full warps however the charts cross a row.
+constexpr uint32_t TS_TILE = 4096;
 // T0/T1: compile-time noise types of the synthetic program's layers (synth_texel)
 template<bool SYNTH, int T0 = -1, int T1 = -1>
 __global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_t W, uint32_t H, const int *__restrict__ owner,
 	const ModesDesc *__restrict__ Mp, const up_synth_program P, int purpose, float *__restrict__ img, int ach) {
+	__shared__ uint16_t cov[TS_TILE];
+	__shared__ uint32_t ncov;
 	const int nch = ach + 3;
 	const uint64_t n = (uint64_t)W * H;
-	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (uint64_t)gridDim.x * blockDim.x) {
-		float *o = img + q * nch;
-		const int t = owner[q];
-		if (t < 0) {
-			for (int c = 0; c < nch; c++) o[c] = NAN;
-			continue;
+	const uint64_t ntiles = (n + TS_TILE - 1) / TS_TILE;
+	const uint32_t lane = threadIdx.x & 31;
+	for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+		if (threadIdx.x == 0) ncov = 0;
+		__syncthreads();
+		const uint64_t q0 = tile * TS_TILE;
+		#pragma unroll 1
+		for (uint32_t it = threadIdx.x; it < TS_TILE; it += blockDim.x) { // every thread the same trip count
+			const uint64_t q = q0 + it;
+			bool covered = false;
+			if (q < n) {
+				covered = owner[q] >= 0;
+				if (!covered) {
+					float *o = img + q * nch;
+					for (int c = 0; c < nch; c++) o[c] = NAN;
+				}
+			}
+			const unsigned mk = __ballot_sync(0xFFFFFFFFu, covered);
+			uint32_t slot = 0;
+			if (lane == 0 && mk) slot = atomicAdd(&ncov, (uint32_t)__popc(mk));
+			slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+			if (covered) cov[slot + __popc(mk & ((1u << lane) - 1u))] = (uint16_t)it;
 		}
-		FixTri f;
-		tri_fixed(m, (uint64_t)t, W, H, f);
-		long long e[3];
-		const uint32_t x = (uint32_t)(q % W), y = (uint32_t)(q / W);
-		tri_cover(f, (long long)x * 256 + 128, (long long)y * 256 + 128, e);
-		// barycentric weights from the exact edge functions: FP64 for the
-		// position (one reciprocal of the area), FP32 for the normal (its
-		// direction does not depend on the area)
-		const double ia = 1.0 / (double)f.area;
-		double w[3];
-		float wf[3];
-		#pragma unroll
-		for (int k = 0; k < 3; k++) {
-			w[f.o[k]] = (double)e[k] * ia;
-			wf[f.o[k]] = (float)e[k];
-		}
-		double p[3] = {0, 0, 0};
-		V3f nsum = zero3();
-		#pragma unroll
-		for (int k = 0; k < 3; k++) {
-			const uint64_t v = m.idx[3 * (uint64_t)t + k];
+		__syncthreads();
+		const uint32_t nc = ncov;
+		#pragma unroll 1
+		for (uint32_t e = threadIdx.x; e < nc; e += blockDim.x) {
+			const uint64_t q = q0 + cov[e];
+			float *o = img + q * nch;
+			const int t = owner[q];
+			FixTri f;
+			tri_fixed(m, (uint64_t)t, W, H, f);
+			long long ed[3];
+			const uint32_t x = (uint32_t)(q % W), y = (uint32_t)(q / W);
+			tri_cover(f, (long long)x * 256 + 128, (long long)y * 256 + 128, ed);
+			// barycentric weights from the exact edge functions: FP64 for the
+			// position (one reciprocal of the area), FP32 for the normal (its
+			// direction does not depend on the area)
+			const double ia = 1.0 / (double)f.area;
+			double w[3];
+			float wf[3];
 			#pragma unroll
-			for (int a = 0; a < 3; a++) p[a] += (double)m.pos[3 * v + a] * w[k];
-			if (!SYNTH) nsum = nsum + v3(m.nrm[3 * v], m.nrm[3 * v + 1], m.nrm[3 * v + 2]) * wf[k];
+			for (int k = 0; k < 3; k++) {
+				w[f.o[k]] = (double)ed[k] * ia;
+				wf[f.o[k]] = (float)ed[k];
+			}
+			double p[3] = {0, 0, 0};
+			V3f nsum = zero3();
+			#pragma unroll
+			for (int k = 0; k < 3; k++) {
+				const uint64_t v = m.idx[3 * (uint64_t)t + k];
+				#pragma unroll
+				for (int a = 0; a < 3; a++) p[a] += (double)m.pos[3 * v + a] * w[k];
+				if (!SYNTH) nsum = nsum + v3(m.nrm[3 * v], m.nrm[3 * v + 1], m.nrm[3 * v + 2]) * wf[k];
+			}
+			const V3f pf = v3((float)p[0], (float)p[1], (float)p[2]);
+			const V3f nf = SYNTH ? zero3() : nsum * (1.f / sqrtf(dot(nsum, nsum)));
+			V3f albedo;
+			float rough, metal = 0.f, height, opacity = 1.f;
+			if (SYNTH) {
+				synth_texel<T0, T1>(P, pf, albedo, rough, height);
+			} else {
+				TileD tl = tile_init(pf, nf, purpose);
+				color_tile(*Mp, tl);
+				albedo = tl.albedo; rough = tl.roughness; metal = tl.metallic; height = tl.height; opacity = tl.opacity;
+			}
+			o[0] = albedo.x; o[1] = albedo.y; o[2] = albedo.z;
+			if (ach == 4) o[3] = opacity;
+			o[ach] = rough; o[ach + 1] = metal; o[ach + 2] = height;
 		}
-		const V3f pf = v3((float)p[0], (float)p[1], (float)p[2]);
-		const V3f nf = SYNTH ? zero3() : nsum * (1.f / sqrtf(dot(nsum, nsum)));
-		V3f albedo;
-		float rough, metal = 0.f, height, opacity = 1.f;
-		if (SYNTH) {
-			synth_texel<T0, T1>(P, pf, albedo, rough, height);
-		} else {
-			TileD tl = tile_init(pf, nf, purpose);
-			color_tile(*Mp, tl);
-			albedo = tl.albedo; rough = tl.roughness; metal = tl.metallic; height = tl.height; opacity = tl.opacity;
-		}
-		o[0] = albedo.x; o[1] = albedo.y; o[2] = albedo.z;
-		if (ach == 4) o[3] = opacity;
-		o[ach] = rough; o[ach + 1] = metal; o[ach + 2] = height;
+		__syncthreads(); // the list is read before the next tile's
 	}
 }
 
@@ -307,15 +339,16 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 		L++;
 	}
 	up_synth_program P{};
+	const uint64_t nsh = (n + TS_TILE - 1) / TS_TILE * 128; // one block per tile at most
 	if (synth) {
 		P = *synth;
 		if (spec_of(P) == SPEC_PERLIN_CELL)
-			tex_shade_kernel<true, 2, CELL_EU_SUB><<<blocks_for((const void *)tex_shade_kernel<true, 2, CELL_EU_SUB>, 128, n), 128, 0, s>>>(m, W, H,
+			tex_shade_kernel<true, 2, CELL_EU_SUB><<<blocks_for((const void *)tex_shade_kernel<true, 2, CELL_EU_SUB>, 128, nsh), 128, 0, s>>>(m, W, H,
 				owner, M, P, purpose, img0, ach);
 		else
-			tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+			tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, nsh), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
 	} else {
-		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, n), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, nsh), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
 	}
 	L++;
 	if (dilation > 0 && dilation <= DT_MAX_ROUNDS) {
