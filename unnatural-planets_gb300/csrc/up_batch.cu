@@ -243,12 +243,14 @@ __global__ void __launch_bounds__(128) batch_qef_kernel(const up_synth_program *
 			fb_list[atomicAdd(fb_count, 1u)] = q;
 	}
 }
-__global__ void __launch_bounds__(128) batch_qef_fp64_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
+// one cell per one-warp block, as dc_qef_fp64_kernel
+__global__ void __launch_bounds__(32) batch_qef_fp64_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
 	const uint32_t *__restrict__ off, uint32_t nchunks, const float *__restrict__ d, const uint32_t *__restrict__ cell_list,
 	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos,
 	const uint32_t *__restrict__ fb_list, const uint32_t *__restrict__ fb_count) {
 	const uint32_t n = *fb_count;
-	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+	if (threadIdx.x != 0) return;
+	for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
 		const uint32_t q = fb_list[e];
 		const uint32_t c = find_chunk(off, nchunks, q);
 		const BatchChunkDev &ch = chunks[c];
@@ -355,7 +357,7 @@ static cudaError_t enqueue_back(BatchState &S, cudaStream_t s) {
 	if ((e = cudaMemsetAsync(fb_count, 0, 4, s)) != cudaSuccess) return e;
 	batch_qef_kernel<<<grid_of((const void *)batch_qef_kernel, 128, S.ncells), 128, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks, S.grid.as<float>(),
 		S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<float>(), S.en.as<float>(), S.pos.as<float>(), S.fb.as<uint32_t>(), fb_count);
-	batch_qef_fp64_kernel<<<grid_of((const void *)batch_qef_fp64_kernel, 128, S.ncells), 128, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks,
+	batch_qef_fp64_kernel<<<grid_of((const void *)batch_qef_fp64_kernel, 1, S.ncells), 32, 0, s>>>(P, C, S.off.as<uint32_t>(), S.nchunks,
 		S.grid.as<float>(), S.clist.as<uint32_t>(), S.emap.as<uint32_t>(), S.et.as<float>(), S.en.as<float>(), S.pos.as<float>(), S.fb.as<uint32_t>(),
 		fb_count);
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;

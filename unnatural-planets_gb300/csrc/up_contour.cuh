@@ -470,13 +470,17 @@ __global__ void __launch_bounds__(256) dc_normal_kernel(const E ev, const float 
 		o[2] = s.g.z * il;
 	}
 }
+// One cell per block (thread 0 of a one-warp block): the FP64 pipe is an
+// SM-wide resource on this part, so the few FP64 cells are spread over as
+// many SMs as there are cells (timed against 32 and 128 cells per block).
 template<class E>
-__global__ void __launch_bounds__(128) dc_qef_fp64_kernel(const E ev, const float *__restrict__ d, const GridDev g,
+__global__ void __launch_bounds__(32) dc_qef_fp64_kernel(const E ev, const float *__restrict__ d, const GridDev g,
 	const uint32_t *__restrict__ cell_list, const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t,
 	const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm, const uint32_t *__restrict__ fb_list,
 	const uint32_t *__restrict__ fb_count) {
 	const uint32_t n = *fb_count;
-	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+	if (threadIdx.x != 0) return;
+	for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
 		const uint32_t c = fb_list[e], p = cell_list[c];
 		double vd[3];
 		dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
@@ -513,8 +517,8 @@ cudaError_t dc_geometry_t(const E &ev, const float *d, const GridDev &g, DcScrat
 		if ((e = cudaEventRecord(S.ev_fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(S.side, S.ev_fork, 0)) != cudaSuccess) return e;
 		s64 = S.side;
 	}
-	const int b64 = persistent_blocks((const void *)dc_qef_fp64_kernel<E>, 128);
-	dc_qef_fp64_kernel<E><<<need < (uint32_t)b64 ? need : (uint32_t)b64, 128, 0, s64>>>(ev, d, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
+	const int b64 = persistent_blocks((const void *)dc_qef_fp64_kernel<E>, 32);
+	dc_qef_fp64_kernel<E><<<ncells < (uint32_t)b64 ? ncells : (uint32_t)b64, 32, 0, s64>>>(ev, d, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
 		nrm, S.fb_list, fb_count);
 	if (nrm) {
 		const int bn = persistent_blocks((const void *)dc_normal_kernel<E>, 256);
