@@ -405,15 +405,30 @@ UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename 
 }
 
 // one run: base shape plus layers into acc (R must be a multiple of CELL_SUB).
-// band > 0: when every sample of the warp's task has |base| > band, the layers
-// are skipped and acc holds the base (the narrow band of contouring: such
-// samples have the sign of the base and are not ends of sign-change edges)
+// band > 0 (narrow band of contouring, values only): when every sample of the
+// warp's task has |base| > band, the layers are skipped and acc holds the
+// base (such samples have the sign of the base and are not ends of
+// sign-change edges: contouring reads only their signs). A lane whose whole
+// run lies that far (|base| at the run's midpoint above band + half the run:
+// the base shapes are 1-Lipschitz) stores the midpoint's value for all its
+// samples, which has their sign, without evaluating the base per sample.
 template<bool GRAD, int T0, int T1>
 UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride, float band = 0.f) {
 	bool far = band > 0.f;
-	const uint32_t spheres = synth_segment_spheres(P, rc.px(0), rc.px(R - 1), rc.py, rc.pz);
+	const float x0 = rc.px(0), x1 = rc.px(R - 1);
+	const uint32_t spheres = synth_segment_spheres(P, x0, x1, rc.py, rc.pz);
+	bool filled = false;
+	if (!GRAD && band > 0.f) {
+		const float xm = 0.5f * (x0 + x1), half = 0.5f * (x1 - x0);
+		const float bm = synth_base<false>(P, v3(xm, rc.py, rc.pz), spheres).v;
+		if (fabsf(bm) > (band + half) * 1.001f + 1e-5f) {
+			#pragma unroll 1
+			for (int r = 0; r < R; r++) acc_set(acc, r * stride, bm, 0.f, 0.f, 0.f);
+			filled = true;
+		}
+	}
 	#pragma unroll 1
-	for (int r = 0; r < R; r++) {
+	for (int r = 0; r < R && !filled; r++) {
 		const NG b = synth_base<GRAD>(P, v3(rc.px(r), rc.py, rc.pz), spheres);
 		acc_set(acc, r * stride, b.v, b.g.x, b.g.y, b.g.z);
 		far = far && fabsf(b.v) > band;
