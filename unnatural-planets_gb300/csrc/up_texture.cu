@@ -205,7 +205,7 @@ constexpr int DT_X = 32, DT_Y = 16, DT_MAX_ROUNDS = 16;
 constexpr uint8_t DT_ABSENT = 254, DT_NAN = 255;
 __host__ __device__ inline size_t dilate_smem(int rounds, int nch) {
 	const size_t t = (size_t)(DT_X + 2 * rounds) * (DT_Y + 2 * rounds);
-	return sizeof(float) * t * nch + ((t + 15) & ~(size_t)15) + sizeof(uint32_t) * t;
+	return sizeof(float) * t * (nch | 1) + ((t + 15) & ~(size_t)15) + sizeof(uint32_t) * t;
 }
 template<int RT>
 __global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__restrict__ img, uint32_t W, uint32_t H, int nch, int ach, int rounds_rt,
@@ -216,7 +216,8 @@ __global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__re
 	const int rounds = RT > 0 ? RT : rounds_rt;
 	const int SX = DT_X + 2 * rounds, SY = DT_Y + 2 * rounds;
 	float *A = dsm;
-	uint8_t *tag = (uint8_t *)(dsm + (size_t)SX * SY * nch);
+	const int NS = nch | 1; // odd texel stride in shared memory: conflict-free
+	uint8_t *tag = (uint8_t *)(dsm + (size_t)SX * SY * NS);
 	uint32_t *list = (uint32_t *)(tag + ((SX * SY + 15) & ~15)); // (ly << 16) | lx of the NaN texels
 	const int x0 = (int)(blockIdx.x * DT_X) - rounds, y0 = (int)(blockIdx.y * DT_Y) - rounds;
 	const unsigned lane = threadIdx.x & 31;
@@ -230,7 +231,17 @@ __global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__re
 			const int gx = x0 + lx, gy = y0 + ly;
 			const bool in = gx >= 0 && gy >= 0 && gx < (int)W && gy < (int)H;
 			const float *src = img + ((uint64_t)(in ? gy : 0) * W + (in ? gx : 0)) * nch;
-			for (int c = 0; c < nch; c++) A[i * nch + c] = in ? src[c] : NAN;
+			if (nch == 6) {
+				const float2 *s2 = (const float2 *)src;
+				#pragma unroll
+				for (int c = 0; c < 3; c++) {
+					const float2 v = in ? s2[c] : make_float2(NAN, NAN);
+					A[i * NS + 2 * c] = v.x;
+					A[i * NS + 2 * c + 1] = v.y;
+				}
+			} else {
+				for (int c = 0; c < nch; c++) A[i * NS + c] = in ? src[c] : NAN;
+			}
 			const uint8_t t = !in ? DT_ABSENT : (isnan(src[0]) ? DT_NAN : 0);
 			tag[i] = t;
 			empty = t == DT_NAN && lx >= 1 && lx < SX - 1 && ly >= 1 && ly < SY - 1;
@@ -256,13 +267,13 @@ __global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__re
 					if (!dx && !dy) continue;
 					const int ni = (ly + dy) * SX + lx + dx;
 					if (tag[ni] >= k) continue; // not valid before this round (or absent)
-					const float *r = A + ni * nch;
+					const float *r = A + ni * NS;
 					for (int c = 0; c < nch; c++) acc[c] += r[c];
 					cnt++;
 				}
 			if (!cnt) continue;
 			const float ic = 1.f / (float)cnt;
-			for (int c = 0; c < nch; c++) A[i * nch + c] = acc[c] * ic;
+			for (int c = 0; c < nch; c++) A[i * NS + c] = acc[c] * ic;
 			tag[i] = (uint8_t)k;
 		}
 		__syncthreads();
@@ -270,7 +281,7 @@ __global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__re
 	for (int j = threadIdx.x; j < DT_X * DT_Y; j += blockDim.x) {
 		const int gx = (int)(blockIdx.x * DT_X) + j % DT_X, gy = (int)(blockIdx.y * DT_Y) + j / DT_X;
 		if (gx >= (int)W || gy >= (int)H) continue;
-		const float *v = A + ((rounds + j / DT_X) * SX + rounds + j % DT_X) * nch;
+		const float *v = A + ((rounds + j / DT_X) * SX + rounds + j % DT_X) * NS;
 		const uint64_t q = (uint64_t)gy * W + gx;
 		for (int c = 0; c < ach; c++) {
 			if (a8) a8[q * ach + c] = to_u8(v[c]);
