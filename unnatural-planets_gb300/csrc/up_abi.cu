@@ -23,7 +23,7 @@ float modes_contour_band(const ModesDesc &D, int field, const float step[3]);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag,
 	cudaStream_t s);
 cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int purpose, const float *pos, const float *nrm, const float *uv,
-	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, int *owner, float *img0, float *img1, uint8_t *a8, uint8_t *s8,
+	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, int *owner, double *tri_ia, float *img0, float *img1, uint8_t *a8, uint8_t *s8,
 	uint8_t *h8, float *af, float *sf, float *hf, int *launches, cudaStream_t s);
 cudaError_t tiles_run(const ModesDesc *M, int purpose, const float *pos, const float *nrm, uint64_t n, float *out11, uint8_t *bt, cudaStream_t s);
 void batch_state_free(void *p);
@@ -38,7 +38,7 @@ enum BufSlot {
 	B_IN0, B_OUT0, B_OUT1, B_OUT2, B_GRAD, B_GRID, B_PARTIALS, B_W,
 	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS, B_DC_FB, B_DC_FBF,
 	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
-	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9,
+	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9, B_TEXIA,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
 	B_BASE_POS, B_BASE_NRM, B_BASE_IDX, B_BASE_ELEV, B_BASE_PARENT, B_BASE_LABEL, B_BASE_CNT, B_BASE_NEWIDX, B_BASE_BLK, B_BASE_SMALL,
 	B_BASE_KEEPV, B_BASE_VALID2, B_BASE_KEEPT, B_PIPE0, B_PIPE1,
@@ -705,6 +705,7 @@ int up_texture(up_context *ctx, int purpose, const up_mesh_in *mesh, uint32_t wi
 		const float *uv = (const float *)stage_in(ctx, B_TEX2, mesh->uvs, V * 8);
 		const uint32_t *idx = (const uint32_t *)stage_in(ctx, B_TEX3, mesh->indices, I * 4);
 		int *owner = (int *)buf(ctx, B_TEX4, n * 4);
+		double *tri_ia = (double *)buf(ctx, B_TEXIA, (I / 3) * 8);
 		float *img0 = (float *)buf(ctx, B_TEX5, n * (ach + 3) * 4);
 		float *img1 = dilation > 0 ? (float *)buf(ctx, B_TEX6, n * (ach + 3) * 4) : nullptr;
 		uint8_t *a8 = (uint8_t *)stage_out(ctx, B_TEX7, out->albedo, n * ach);
@@ -714,7 +715,7 @@ int up_texture(up_context *ctx, int purpose, const up_mesh_in *mesh, uint32_t wi
 		float *sf = (float *)stage_out(ctx, B_BATCH1, out->special_f32, n * 8);
 		float *hf = (float *)stage_out(ctx, B_BATCH2, out->height_f32, n * 4);
 		check(texture_run(ctx->synthetic ? nullptr : ctx->d_modes, ctx->synthetic ? &ctx->prog : nullptr, purpose, pos, nrm, uv, idx, I,
-			width, height, dilation, owner, img0, img1, a8, s8, h8, af, sf, hf, nullptr, ctx->stream), "texture kernels");
+			width, height, dilation, owner, tri_ia, img0, img1, a8, s8, h8, af, sf, hf, nullptr, ctx->stream), "texture kernels");
 		finish_out(ctx, out->albedo, a8, n * ach);
 		finish_out(ctx, out->special, s8, n * 2);
 		finish_out(ctx, out->height, h8, n);

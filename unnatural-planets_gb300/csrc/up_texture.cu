@@ -52,10 +52,13 @@ __device__ __forceinline__ bool tri_cover(const FixTri &f, long long px, long lo
 	return edge_in(e[0], f.cx - f.bx, f.cy - f.by) && edge_in(e[1], f.ax - f.cx, f.ay - f.cy) && edge_in(e[2], f.bx - f.ax, f.by - f.ay);
 }
 
-__global__ void __launch_bounds__(256) tex_raster_kernel(const TexMesh m, uint32_t W, uint32_t H, int *__restrict__ owner) {
+// (also the FP64 reciprocal of each triangle's area, for the shading of its
+// texels: one division per triangle instead of one per texel)
+__global__ void __launch_bounds__(256) tex_raster_kernel(const TexMesh m, uint32_t W, uint32_t H, int *__restrict__ owner, double *__restrict__ tri_ia) {
 	for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m.ntri; t += (uint64_t)gridDim.x * blockDim.x) {
 		FixTri f;
 		if (!tri_fixed(m, t, W, H, f)) continue;
+		tri_ia[t] = 1.0 / (double)f.area;
 		const long long xmin = min(f.ax, min(f.bx, f.cx)), xmax = max(f.ax, max(f.bx, f.cx));
 		const long long ymin = min(f.ay, min(f.by, f.cy)), ymax = max(f.ay, max(f.by, f.cy));
 		// texel x is covered only if x*256 + 128 lies in [xmin, xmax]
@@ -78,7 +81,7 @@ constexpr uint32_t TS_TILE = 4096;
 // T0/T1: compile-time noise types of the synthetic program's layers (synth_texel)
 template<bool SYNTH, int T0 = -1, int T1 = -1>
 __global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_t W, uint32_t H, const int *__restrict__ owner,
-	const ModesDesc *__restrict__ Mp, const up_synth_program P, int purpose, float *__restrict__ img, int ach) {
+	const double *__restrict__ tri_ia, const ModesDesc *__restrict__ Mp, const up_synth_program P, int purpose, float *__restrict__ img, int ach) {
 	__shared__ uint16_t cov[TS_TILE];
 	__shared__ uint32_t ncov;
 	const int nch = ach + 3;
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(128) tex_shade_kernel(const TexMesh m, uint32_
 			// barycentric weights from the exact edge functions: FP64 for the
 			// position (one reciprocal of the area), FP32 for the normal (its
 			// direction does not depend on the area)
-			const double ia = 1.0 / (double)f.area;
+			const double ia = tri_ia[t];
 			double w[3];
 			float wf[3];
 			#pragma unroll
@@ -336,7 +339,7 @@ static int blocks_for(const void *k, int threads, uint64_t work) {
 }
 
 cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int purpose, const float *pos, const float *nrm, const float *uv,
-	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, int *owner, float *img0, float *img1, uint8_t *a8, uint8_t *s8,
+	const uint32_t *idx, uint64_t nidx, uint32_t W, uint32_t H, int dilation, int *owner, double *tri_ia, float *img0, float *img1, uint8_t *a8, uint8_t *s8,
 	uint8_t *h8, float *af, float *sf, float *hf, int *launches, cudaStream_t s) {
 	const uint64_t n = (uint64_t)W * H;
 	const int ach = purpose == UP_PURPOSE_WATER ? 4 : 3;
@@ -346,7 +349,7 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 	if (e != cudaSuccess) return e;
 	int L = 0;
 	if (m.ntri) {
-		tex_raster_kernel<<<blocks_for((const void *)tex_raster_kernel, 256, m.ntri), 256, 0, s>>>(m, W, H, owner);
+		tex_raster_kernel<<<blocks_for((const void *)tex_raster_kernel, 256, m.ntri), 256, 0, s>>>(m, W, H, owner, tri_ia);
 		L++;
 	}
 	up_synth_program P{};
@@ -355,11 +358,11 @@ cudaError_t texture_run(const ModesDesc *M, const up_synth_program *synth, int p
 		P = *synth;
 		if (spec_of(P) == SPEC_PERLIN_CELL)
 			tex_shade_kernel<true, 2, CELL_EU_SUB><<<blocks_for((const void *)tex_shade_kernel<true, 2, CELL_EU_SUB>, 128, nsh), 128, 0, s>>>(m, W, H,
-				owner, M, P, purpose, img0, ach);
+				owner, tri_ia, M, P, purpose, img0, ach);
 		else
-			tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, nsh), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+			tex_shade_kernel<true><<<blocks_for((const void *)tex_shade_kernel<true>, 128, nsh), 128, 0, s>>>(m, W, H, owner, tri_ia, M, P, purpose, img0, ach);
 	} else {
-		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, nsh), 128, 0, s>>>(m, W, H, owner, M, P, purpose, img0, ach);
+		tex_shade_kernel<false><<<blocks_for((const void *)tex_shade_kernel<false>, 128, nsh), 128, 0, s>>>(m, W, H, owner, tri_ia, M, P, purpose, img0, ach);
 	}
 	L++;
 	if (dilation > 0 && dilation <= DT_MAX_ROUNDS) {
