@@ -7,6 +7,7 @@
 #include "../../unnatural-planets_gb300/csrc/up_modes.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_modes_runs.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_coloring.cuh"
+#include "../../unnatural-planets_gb300/csrc/up_fastdiv.h"
 #include <string>
 
 namespace up {
@@ -195,6 +196,12 @@ uint32_t hc_segment_base(const up_synth_program *P, float x0, float x1, float y,
 		out_f[4 * r] = b.v; out_f[4 * r + 1] = b.g.x; out_f[4 * r + 2] = b.g.y; out_f[4 * r + 3] = b.g.z;
 	}
 	return live;
+}
+
+// FastDiv (up_fastdiv.h): q[i] = n[i] / d by the multiply-shift
+void hc_fastdiv(uint32_t d, const uint32_t *n, uint64_t count, uint32_t *q) {
+	const FastDiv f = FastDiv::of(d);
+	for (uint64_t i = 0; i < count; i++) q[i] = f.div(n[i]);
 }
 }
 

@@ -214,3 +214,19 @@ def test_segment_sphere_culling_is_exact(H):
         dropped += P.n_spheres - bin(live & ((1 << P.n_spheres) - 1)).count("1")
     assert dropped > 4000 * P.n_spheres // 2
 
+
+def test_fastdiv_exact(H):
+    """The multiply-shift division by a fixed divisor (up_fastdiv.h, used for
+    the chunk dimensions of batches) equals integer division for divisors
+    1 .. 4096, powers of two and large values, on edge and random dividends."""
+    H.hc_fastdiv.argtypes = [C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p]
+    r = np.random.default_rng(8)
+    divisors = list(range(1, 4097)) + [2 ** k for k in range(32)] + [2 ** k + 1 for k in range(1, 31)] + [2 ** 32 - 1, 2 ** 31 - 1]
+    divisors += [int(x) for x in r.integers(1, 2 ** 32, size=200)]
+    for d in divisors:
+        n = np.concatenate([np.array([0, 1, d - 1, d, d + 1, 2 ** 32 - 1, 2 ** 32 - 2], dtype=np.uint64) % 2 ** 32,
+                            r.integers(0, 2 ** 32, size=64, dtype=np.uint64)]).astype(np.uint32)
+        q = np.empty_like(n)
+        H.hc_fastdiv(d, n.ctypes.data, len(n), q.ctypes.data)
+        assert np.array_equal(q, n // np.uint32(d)), d
+

@@ -19,29 +19,12 @@
 // Batches of chunks run the same word kernels per chunk (up_batch.cu).
 #pragma once
 #include "up_internal.h"
+#include "up_fastdiv.h"
 #include "up_noise.cuh"
 
 namespace up {
 
 constexpr int DC_T = 256, DC_ITEMS = 4, DC_PB = DC_T * DC_ITEMS;
-
-// n / d for a divisor fixed per chunk: the round-up multiply-shift of
-// Granlund and Montgomery (PLDI 1994), exact for every 32-bit n
-struct FastDiv {
-	uint32_t d, m, s;
-	static FastDiv of(uint32_t d) {
-		FastDiv f{d, 0, 0};
-		uint32_t l = 0;
-		while (l < 32 && (1ull << l) < d) l++; // ceil(log2 d)
-		f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
-		f.s = l > 0 ? l - 1 : 0;
-		return f;
-	}
-	__device__ __forceinline__ uint32_t div(uint32_t n) const {
-		const uint32_t t = __umulhi(m, n);
-		return d == 1 ? n : (t + ((n - t) >> 1)) >> s;
-	}
-};
 
 __device__ __forceinline__ float dc_coord(const GridDev &g, int a, uint32_t i) {
 	return __fadd_rn(__fmul_rn((float)i, g.step[a]), g.lo[a]);
