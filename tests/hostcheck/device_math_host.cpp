@@ -118,6 +118,27 @@ void hc_synth_texel(const up_synth_program *P, const float *pos, uint64_t n, flo
 float hc_noise_bound(int type, int dist, int op) { return noise_abs_bound(type, dist, op); }
 float hc_synth_noise_bound(const up_synth_program *P) { return synth_noise_bound(*P); }
 
+// value-only runs with a narrow band (the internal sampling of contouring)
+void hc_grid_runs_band(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float band, float *out) {
+	constexpr int R = RUN_R;
+	constexpr int T1 = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);
+	auto coord = [&](int a, uint32_t i) { volatile float m = (float)i * step[a]; return m + lo[a]; };
+	RunCtx rc;
+	rc.lo_x = lo[0];
+	rc.step_x = step[0];
+	rc.nx = n[0];
+	for (uint32_t k = 0; k < n[2]; k++)
+		for (uint32_t j = 0; j < n[1]; j++)
+			for (uint32_t i0 = 0; i0 < n[0]; i0 += R) {
+				rc.i0 = i0;
+				rc.py = coord(1, j);
+				rc.pz = coord(2, k);
+				float acc[R];
+				synth_run<false, 2, T1>(*P, rc, R, acc, 1, band);
+				for (int r = 0; r < R && i0 + r < n[0]; r++) out[((uint64_t)k * n[1] + j) * n[0] + i0 + r] = acc[r];
+			}
+}
+
 void hc_grid_runs(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float *out, float *grad) {
 	constexpr int R = RUN_R;
 	constexpr int T1 = cell_spec(UP_DIST_EUCLIDEAN, UP_OP_SUBTRACT);

@@ -230,3 +230,37 @@ def test_fastdiv_exact(H):
         H.hc_fastdiv(d, n.ctypes.data, len(n), q.ctypes.data)
         assert np.array_equal(q, n // np.uint32(d)), d
 
+
+def test_narrow_band_runs_keep_signs(H, O):
+    """The narrow-band runs of contouring (synth_run with a band, compiled for
+    the host; there a run is one task): every sample keeps the sign of the
+    exactly sampled grid; the samples whose base lies inside the band keep
+    their exact values; the rest (runs filled from their midpoint, or whose
+    layers were skipped) lie outside the band. Many runs are filled."""
+    H.hc_grid_runs_band.argtypes = [C.POINTER(_abi().SynthProgram), C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+    W = workloads()
+    P = W.torus_spheres_ridged_cellular()
+    n = (96, 64, 56)
+    g = W.grid(W.GRID_C2, n=n)
+    lo = np.array(g.lo[:], np.float32)
+    st = np.array([(g.hi[a] - g.lo[a]) / np.float32(g.n[a] - 1) for a in range(3)], np.float32)
+    nn = np.array(n, np.uint32)
+    band = np.float32((H.hc_synth_noise_bound(C.byref(P)) + st.max()) * 1.001 + 1e-5)
+    full = np.empty(g.count, np.float32)
+    H.hc_grid_runs(C.byref(P), lo.ctypes.data, st.ctypes.data, nn.ctypes.data, full.ctypes.data, None)
+    banded = np.empty(g.count, np.float32)
+    H.hc_grid_runs_band(C.byref(P), lo.ctypes.data, st.ctypes.data, nn.ctypes.data, band, banded.ctypes.data)
+    assert np.array_equal(banded < 0, full < 0)
+    # base values: the program without its layers
+    P0 = W.torus_spheres_ridged_cellular()
+    P0.n_layers = 0
+    base = np.empty(g.count, np.float32)
+    H.hc_grid_runs(C.byref(P0), lo.ctypes.data, st.ctypes.data, nn.ctypes.data, base.ctypes.data, None)
+    inside = np.abs(base) <= band
+    assert inside.any() and np.array_equal(banded[inside], full[inside])
+    changed = banded != full
+    assert changed.mean() > 0.5 and np.all(np.abs(base[changed]) > band)
+    # filled runs: 16 equal values where the base varies along the run
+    rows = banded.reshape(-1, n[0])[:, :96].reshape(-1, 6, 16)
+    assert (np.ptp(rows, axis=2) == 0).mean() > 0.5
+
