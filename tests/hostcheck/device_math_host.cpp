@@ -192,8 +192,10 @@ int hc_modes_grid_runs(void *d, const float *lo, const float *step, const uint32
 				if (M.elevation == 2) modes_run_fill<2>(M, rc, R, tab, 1);
 				else if (M.elevation == 3) modes_run_fill<3>(M, rc, R, tab, 1);
 				else modes_run_fill<4>(M, rc, R, tab, 1);
+				float shv[R];
+				modes_run_shape(M, rc, R, band, shv, 1);
 				for (int r = 0; r < R && i0 + r < n[0]; r++) {
-					const float sh = shape_eval(M, vs(rc.px(r), rc.py, rc.pz));
+					const float sh = shv[r];
 					float v[3];
 					if (M.elevation == 2) modes_run_fields<2>(M, rc, r, sh, true, band, tab, 1, v);
 					else if (M.elevation == 3) modes_run_fields<3>(M, rc, r, sh, true, band, tab, 1, v);

@@ -264,3 +264,35 @@ def test_narrow_band_runs_keep_signs(H, O):
     rows = banded.reshape(-1, n[0])[:, :96].reshape(-1, 6, 16)
     assert (np.ptp(rows, axis=2) == 0).mean() > 0.5
 
+
+def test_modes_narrow_band_runs_keep_signs(H, O):
+    """The reference-mode narrow band over runs (modes_run_shape, host form of
+    the x-coherent kernel): land keeps the exact grid's signs, the samples of
+    shape inside the band keep their exact values, and runs are filled."""
+    H.hc_modes_create.restype = C.c_void_p
+    H.hc_modes_create.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_uint32]
+    H.hc_modes_free.argtypes = [C.c_void_p]
+    H.hc_modes_band.restype = C.c_float
+    H.hc_modes_band.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    H.hc_modes_grid_runs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    d = H.hc_modes_create(b"sphere", b"lakes", b"default", 0, 0, 4)
+    n = (96, 50, 40)
+    g = _abi().Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), n)
+    lo = np.array(g.lo[:], np.float32)
+    st = np.array([(g.hi[a] - g.lo[a]) / np.float32(g.n[a] - 1) for a in range(3)], np.float32)
+    nn = np.array(n, np.uint32)
+    band = H.hc_modes_band(d, 0, st.ctypes.data)
+    assert band > 0
+    N = g.count
+    full = [np.empty(N, np.float32) for _ in range(3)]
+    banded = [np.empty(N, np.float32) for _ in range(3)]
+    assert H.hc_modes_grid_runs(d, lo.ctypes.data, st.ctypes.data, nn.ctypes.data, 0.0, *[o.ctypes.data for o in full]) == 1
+    assert H.hc_modes_grid_runs(d, lo.ctypes.data, st.ctypes.data, nn.ctypes.data, band, *[o.ctypes.data for o in banded]) == 1
+    assert np.array_equal(banded[0] < 0, full[0] < 0)
+    shape = full[1]  # water = the shape
+    inside = np.abs(shape) <= band
+    assert inside.any() and np.array_equal(banded[0][inside], full[0][inside])
+    rows = banded[0].reshape(-1, n[0]).reshape(-1, 6, 16)
+    assert (np.ptp(rows, axis=2) == 0).mean() > 0.3
+    H.hc_modes_free(d)
+

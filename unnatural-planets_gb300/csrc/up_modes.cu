@@ -101,27 +101,7 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 		rc.i0 = run * R;
 		rc.py = mgrid_coord(g, 1, j);
 		rc.pz = mgrid_coord(g, 2, k + g.k0);
-		bool far = band > 0.f, filled = false;
-		if (band > 0.f) {
-			// the band is given only for 1-Lipschitz shapes (modes_contour_band):
-			// a run whose midpoint lies further than band + half the run is
-			// outside the band everywhere; its samples take the midpoint's
-			// value (their sign; contouring reads nothing else of them)
-			const float x0 = rc.px(0), x1 = rc.px(R - 1);
-			const float xm = 0.5f * (x0 + x1), half = 0.5f * (x1 - x0);
-			const float sm = shape_eval(M, vs(xm, rc.py, rc.pz));
-			if (fabsf(sm) > (band + half) * 1.001f + 1e-3f * (1.f + fabsf(sm))) {
-				#pragma unroll 1
-				for (int r = 0; r < R; r++) shv[r * MRUNS_T] = sm;
-				filled = true;
-			}
-		}
-		#pragma unroll 1
-		for (int r = 0; r < R && !filled; r++) {
-			const float sh = shape_eval(M, vs(rc.px(r), rc.py, rc.pz));
-			shv[r * MRUNS_T] = sh;
-			far = far && fabsf(sh) > band;
-		}
+		bool far = modes_run_shape(M, rc, R, band, shv, MRUNS_T);
 		far = __all_sync(0xFFFFFFFFu, far); // every lane of the warp runs every task
 		if (need_e && !far) modes_run_fill<EM>(M, rc, R, tab, MRUNS_T);
 		// fields of sample r into slots 0-2 at r (after its table entries are read)

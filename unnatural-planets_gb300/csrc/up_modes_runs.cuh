@@ -69,6 +69,32 @@ template<int EM> UP_HD void modes_run_fill(const ModesDesc &M, const RunCtx &rc,
 	}
 }
 
+// shape values of the run's samples into sh[r * stride]; returns true when
+// every sample lies outside the band (band > 0). The band is given only for
+// 1-Lipschitz shapes (modes_contour_band): a run whose midpoint lies further
+// than band + half the run is outside it everywhere, and its samples take the
+// midpoint's value (their sign; contouring reads nothing else of them).
+UP_HD bool modes_run_shape(const ModesDesc &M, const RunCtx &rc, int R, float band, float *sh, int stride) {
+	if (band > 0.f) {
+		const float x0 = rc.px(0), x1 = rc.px(R - 1);
+		const float xm = 0.5f * (x0 + x1), half = 0.5f * (x1 - x0);
+		const float sm = shape_eval(M, vs(xm, rc.py, rc.pz));
+		if (fabsf(sm) > (band + half) * 1.001f + 1e-3f * (1.f + fabsf(sm))) {
+			#pragma unroll 1
+			for (int r = 0; r < R; r++) sh[r * stride] = sm;
+			return true;
+		}
+	}
+	bool far = band > 0.f;
+	#pragma unroll 1
+	for (int r = 0; r < R; r++) {
+		const float v = shape_eval(M, vs(rc.px(r), rc.py, rc.pz));
+		sh[r * stride] = v;
+		far = far && fabsf(v) > band;
+	}
+	return far;
+}
+
 // land, water, navigation of sample r with shape value sh (fields_of of the
 // per-sample kernel); band > 0 and |sh| > band: every field is sh (narrow
 // band of contouring); need_e false: no field needs the elevation
