@@ -385,6 +385,94 @@ UP_HD NG cellular_n(V3f p, uint32_t key, int dist_rt, int op_rt) {
 	}
 }
 
+// Warp-cooperative cellular_n for per-point kernels whose 32 lanes all call
+// it together (device only). When the lanes' cells span at most two values
+// per axis, the union of their 3x3x3 neighbourhoods fits a 4 x 4 x 4 block:
+// the lanes hash it together (two cells each) into a per-warp shared table of
+// jitters, and each lane reads its 27 candidates from it; otherwise every lane
+// hashes its own, as cellular_n. The candidates, their ids and every
+// arithmetic step are those of cellular_n, so the result is the same bit for
+// bit. Spatially sorted points (neighbours in neighbouring lanes) take the
+// table.
+#ifdef __CUDACC__
+constexpr int PT_WARPS = 8; // warps per block of the kernels that call it
+__shared__ float4 g_pt_cells[PT_WARPS * 64];
+template<bool GRAD, int DIST = -1, int OP = -1>
+__device__ NG cellular_warp(V3f p, uint32_t key, int dist_rt, int op_rt) {
+#ifdef __CUDA_ARCH__
+	const Cell c = cell_of(p);
+	const int x0 = __reduce_min_sync(0xFFFFFFFFu, c.ix), x1 = __reduce_max_sync(0xFFFFFFFFu, c.ix);
+	const int y0 = __reduce_min_sync(0xFFFFFFFFu, c.iy), y1 = __reduce_max_sync(0xFFFFFFFFu, c.iy);
+	const int z0 = __reduce_min_sync(0xFFFFFFFFu, c.iz), z1 = __reduce_max_sync(0xFFFFFFFFu, c.iz);
+	if (x1 - x0 > 1 || y1 - y0 > 1 || z1 - z0 > 1) return cellular_n<GRAD, DIST, OP>(p, key, dist_rt, op_rt); // the same for every lane
+	const int dist = DIST >= 0 ? DIST : dist_rt;
+	const int op = OP >= 0 ? OP : op_rt;
+	float4 *tab = g_pt_cells + (threadIdx.x >> 5) * 64;
+	__syncwarp(); // the previous call's readers are done
+	for (int e = (int)(threadIdx.x & 31); e < 64; e += 32) {
+		const uint32_t h = mix32(((uint32_t)(x0 - 1 + (e >> 4)) * HX) ^ ((uint32_t)(y0 - 1 + ((e >> 2) & 3)) * HY) ^
+			(((uint32_t)(z0 - 1 + (e & 3)) * HZ) ^ key));
+		tab[e] = make_float4(jitter(h, 0), jitter(h, 10), jitter(h, 20), __uint_as_float(h));
+	}
+	__syncwarp();
+	// entry of candidate (dx, dy, dz): ((ix + dx) - x0 + 1) * 16 + ((iy + dy) - y0 + 1) * 4 + (iz + dz) - z0 + 1
+	const int o = (c.ix - x0) * 16 + (c.iy - y0) * 4 + (c.iz - z0);
+	uint32_t K1 = 0xFFFFFFFFu, K2 = 0xFFFFFFFFu;
+	#pragma unroll 1
+	for (int dz = -1; dz <= 1; dz++) {
+		#pragma unroll 1
+		for (int dy = -1; dy <= 1; dy++) {
+			const uint32_t id0 = (uint32_t)((dz + 1) * 9 + (dy + 1) * 3);
+			const int row = o + (dy + 1) * 4 + (dz + 1);
+			#pragma unroll
+			for (int dx = -1; dx <= 1; dx++) {
+				const float4 t = tab[row + (dx + 1) * 16];
+				const float vx = ((float)dx + t.x) - c.fx;
+				const float vy = ((float)dy + t.y) - c.fy;
+				const float vz = ((float)dz + t.z) - c.fz;
+				const uint32_t k = (f_bits(cell_dist<DIST>(vx, vy, vz, dist)) & ~63u) | (id0 + (uint32_t)(dx + 1));
+				K2 = K2 < (K1 > k ? K1 : k) ? K2 : (K1 > k ? K1 : k);
+				K1 = K1 < k ? K1 : k;
+			}
+		}
+	}
+	float F[2];
+	V3f g[2];
+	uint32_t cellh = 0;
+	#pragma unroll
+	for (int w = 0; w < 2; w++) {
+		const uint32_t id = (w ? K2 : K1) & 63u;
+		const int dz = (int)(id / 9u) - 1, dy = (int)((id / 3u) % 3u) - 1, dx = (int)(id % 3u) - 1;
+		const float4 t = tab[o + (dx + 1) * 16 + (dy + 1) * 4 + (dz + 1)];
+		const float vx = ((float)dx + t.x) - c.fx;
+		const float vy = ((float)dy + t.y) - c.fy;
+		const float vz = ((float)dz + t.z) - c.fz;
+		F[w] = cell_dist<DIST>(vx, vy, vz, dist);
+		g[w] = v3(vx, vy, vz);
+		if (w == 0) cellh = __float_as_uint(t.w);
+	}
+	float F1 = F[0], F2 = F[1];
+	if (dist == 0) { F1 = sqrtf(F1); F2 = sqrtf(F2); }
+	V3f dF1 = zero3(), dF2 = zero3();
+	if (GRAD) {
+		dF1 = cell_dist_grad(g[0], F1, dist);
+		dF2 = cell_dist_grad(g[1], F2, dist);
+	}
+	switch (op) {
+		case 0: return ngc(hash_signed(mix32(cellh)));
+		case 1: return ng(F1 - 1.f, dF1);
+		case 2: return ng(F2 - 1.f, dF2);
+		case 3: return ng((F1 + F2) * 0.5f - 1.f, (dF1 + dF2) * 0.5f);
+		case 4: return ng(F2 - F1 - 1.f, dF2 - dF1);
+		case 5: return ng(F1 * F2 * 0.5f - 1.f, (dF1 * F2 + dF2 * F1) * 0.5f);
+		default: return ng(F1 / F2 - 1.f, (dF1 * F2 - dF2 * F1) * (1.f / (F2 * F2)));
+	}
+#else
+	return cellular_n<GRAD, DIST, OP>(p, key, dist_rt, op_rt);
+#endif
+}
+#endif
+
 // ---------------------------------------------------------------- dispatch
 // noise type codes follow up_noise_type in include/up_abi.h; the run-time
 // dispatch is out of line (one copy per translation unit and GRAD)

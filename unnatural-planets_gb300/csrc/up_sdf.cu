@@ -161,13 +161,22 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
 }
 
+// Every lane of a warp runs every step (lanes past n evaluate the last point
+// and store nothing), so the warp-cooperative cellular noise (cellular_warp)
+// can share cell hashes between the lanes of spatially close points.
+static_assert(256 / 32 <= PT_WARPS, "the per-warp cell tables of cellular_warp");
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(256) synth_points_kernel(const up_synth_program P, const float *__restrict__ xyz, uint64_t n,
 	float *__restrict__ out, float *__restrict__ grad, unsigned *__restrict__ nanflag) {
 	bool bad = false;
-	for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (uint64_t)gridDim.x * blockDim.x) {
-		const V3f p = v3(xyz[3 * idx], xyz[3 * idx + 1], xyz[3 * idx + 2]);
-		const NG d = synth_eval<GRAD, T0, T1>(P, p);
+	const uint32_t lane = threadIdx.x & 31;
+	for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += (uint64_t)gridDim.x * blockDim.x) {
+		const uint64_t idx = base + lane;
+		const bool valid = idx < n;
+		const uint64_t q = valid ? idx : n - 1;
+		const V3f p = v3(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]);
+		const NG d = synth_eval<GRAD, T0, T1, true>(P, p);
+		if (!valid) continue;
 		out[idx] = d.v;
 		if (GRAD) {
 			grad[3 * idx] = d.g.x;
@@ -258,13 +267,18 @@ __global__ void __launch_bounds__(BWD_THREADS) synth_bwd_kernel(const up_synth_p
 	float acc[ACC_N];
 	#pragma unroll
 	for (int i = 0; i < ACC_N; i++) acc[i] = 0.f;
-	for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (uint64_t)gridDim.x * blockDim.x) {
+	// every lane of a warp runs every step (as synth_points_kernel)
+	const uint32_t lane0 = threadIdx.x & 31;
+	for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += (uint64_t)gridDim.x * blockDim.x) {
+		const uint64_t idx = base + lane0;
+		const uint64_t q = idx < n ? idx : n - 1;
 		// a point of weight 0 adds w * dd/dtheta = 0 (the derivatives are
-		// finite for finite parameters): a hinge loss leaves most weights 0
-		const float wi = w[idx];
-		if (wi == 0.f) continue;
-		const V3f p = v3(xyz[3 * idx], xyz[3 * idx + 1], xyz[3 * idx + 2]);
-		synth_bwd<T0, T1>(P, p, wi, acc);
+		// finite for finite parameters): a hinge loss leaves most weights 0,
+		// and a warp whose weights are all 0 skips its step
+		const float wi = idx < n ? w[idx] : 0.f;
+		if (__all_sync(0xFFFFFFFFu, wi == 0.f)) continue;
+		const V3f p = v3(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]);
+		synth_bwd<T0, T1, true>(P, p, wi, acc);
 	}
 	// warp sums, then warps in a fixed order: deterministic per block
 	__shared__ float red[BWD_THREADS / 32][ACC_N];

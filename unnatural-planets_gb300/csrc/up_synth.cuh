@@ -15,8 +15,13 @@ namespace up {
 // 0..4 = that noise type; cellular = 5 | (distance + 1) << 4 | (operation + 1) << 8
 constexpr int cell_spec(int dist, int op) { return 5 | ((dist + 1) << 4) | ((op + 1) << 8); }
 
-template<bool GRAD, int TYPE>
+// COOP: the caller's 32 lanes call together (cellular_warp for a
+// compile-time cellular layer; the same results)
+template<bool GRAD, int TYPE, bool COOP = false>
 UP_HD NG noise_t(const up_noise_layer &L, V3f q, uint32_t key) {
+#ifdef __CUDA_ARCH__
+	if (COOP && TYPE >= 0 && (TYPE & 15) == 5) return cellular_warp<GRAD, ((TYPE >> 4) & 15) - 1, ((TYPE >> 8) & 15) - 1>(q, key, L.distance, L.operation);
+#endif
 	if (TYPE >= 0 && (TYPE & 15) == 5) return cellular_n<GRAD, ((TYPE >> 4) & 15) - 1, ((TYPE >> 8) & 15) - 1>(q, key, L.distance, L.operation);
 	const int t = TYPE >= 0 ? TYPE : L.type;
 	if (TYPE == 2 || (TYPE < 0 && t == 2)) { if (GRAD) return perlin_g(q, key); return ngc(perlin_v(q, key)); }
@@ -38,7 +43,7 @@ inline Spec spec_of(const up_synth_program &P) {
 }
 
 // one layer: value and gradient with respect to p
-template<bool GRAD, int TYPE>
+template<bool GRAD, int TYPE, bool COOP = false>
 UP_HD NG layer_eval(const up_noise_layer &L, V3f p) {
 	float v = 0.f;
 	V3f g = zero3();
@@ -46,7 +51,7 @@ UP_HD NG layer_eval(const up_noise_layer &L, V3f p) {
 	#pragma unroll 1
 	for (int i = 0; i < L.octaves; i++) {
 		const float f = L.freq[i];
-		const NG n = noise_t<GRAD, TYPE>(L, p * f, seed_key(L.seed + (uint32_t)i));
+		const NG n = noise_t<GRAD, TYPE, COOP>(L, p * f, seed_key(L.seed + (uint32_t)i));
 		float s = n.v, ds = 1.f;
 		if (ridged) { s = 1.f - 2.f * fabsf(n.v); ds = n.v > 0.f ? -2.f : (n.v < 0.f ? 2.f : 0.f); }
 		v += L.amp[i] * s;
@@ -216,16 +221,16 @@ UP_HD float synth_noise_bound(const up_synth_program &P) {
 }
 
 // full program; T0/T1 = compile-time noise type of layer 0/1 (-1 = runtime)
-template<bool GRAD, int T0, int T1>
+template<bool GRAD, int T0, int T1, bool COOP = false>
 UP_HD NG synth_eval(const up_synth_program &P, V3f p) {
 	NG d = synth_base<GRAD>(P, p);
 	if (P.n_layers > 0) {
-		const NG e = layer_eval<GRAD, T0>(P.layer[0], p);
+		const NG e = layer_eval<GRAD, T0, COOP>(P.layer[0], p);
 		d.v -= e.v;
 		if (GRAD) d.g -= e.g;
 	}
 	if (P.n_layers > 1) {
-		const NG e = layer_eval<GRAD, T1>(P.layer[1], p);
+		const NG e = layer_eval<GRAD, T1, COOP>(P.layer[1], p);
 		d.v -= e.v;
 		if (GRAD) d.g -= e.g;
 	}
@@ -239,14 +244,14 @@ UP_HD NG synth_eval(const up_synth_program &P, V3f p) {
 //   [32]   R or h, [33] r or rr, [34,42) sphere radii, [42] k
 constexpr int ACC_N = 43;
 
-template<int TYPE, int SLOT>
+template<int TYPE, int SLOT, bool COOP = false>
 UP_HD void layer_bwd(const up_noise_layer &L, V3f p, float w, float acc[ACC_N]) {
 	const bool ridged = L.fractal == UP_FRACTAL_RIDGED;
 	#pragma unroll
 	for (int i = 0; i < 8; i++) {
 		if (i < L.octaves) {
 			const float f = L.freq[i];
-			const NG n = noise_t<true, TYPE>(L, p * f, seed_key(L.seed + (uint32_t)i));
+			const NG n = noise_t<true, TYPE, COOP>(L, p * f, seed_key(L.seed + (uint32_t)i));
 			float s = n.v, ds = 1.f;
 			if (ridged) { s = 1.f - 2.f * fabsf(n.v); ds = n.v > 0.f ? -2.f : (n.v < 0.f ? 2.f : 0.f); }
 			acc[SLOT * 16 + i] -= w * s;
@@ -255,10 +260,10 @@ UP_HD void layer_bwd(const up_noise_layer &L, V3f p, float w, float acc[ACC_N]) 
 	}
 }
 
-template<int T0, int T1>
+template<int T0, int T1, bool COOP = false>
 UP_HD void synth_bwd(const up_synth_program &P, V3f p, float w, float acc[ACC_N]) {
-	if (P.n_layers > 0) layer_bwd<T0, 0>(P.layer[0], p, w, acc);
-	if (P.n_layers > 1) layer_bwd<T1, 1>(P.layer[1], p, w, acc);
+	if (P.n_layers > 0) layer_bwd<T0, 0, COOP>(P.layer[0], p, w, acc);
+	if (P.n_layers > 1) layer_bwd<T1, 1, COOP>(P.layer[1], p, w, acc);
 	switch (P.base) {
 		case UP_BASE_SPHERE: acc[32] -= w; break;
 		case UP_BASE_TORUS: {
