@@ -200,6 +200,21 @@ def _shell(planet, n, half_width, seed):
     return torch.cat(got)[:n].contiguous()
 
 
+def _morton_sorted(x):
+    """the points in Morton (Z-curve) order of a 1024^3 grid over the [-1.6, 1.6]^3
+    box: neighbours in space become neighbours in the array (the same set)"""
+    import torch
+    q = ((x + 1.6) * (1023 / 3.2)).clamp(0, 1023).to(torch.int64)
+
+    def spread(v):
+        v = (v | (v << 16)) & 0x030000FF
+        v = (v | (v << 8)) & 0x0300F00F
+        v = (v | (v << 4)) & 0x030C30C3
+        return (v | (v << 2)) & 0x09249249
+    code = spread(q[:, 0]) | (spread(q[:, 1]) << 1) | (spread(q[:, 2]) << 2)
+    return x[torch.argsort(code)].contiguous()
+
+
 def extra_adjoint(up, W, stream):
     """the value+adjoint configuration: the torus + 8 spheres - ridged Perlin +
     cellular planet, 16,777,216 points uniform in its 0.05 shell"""
@@ -208,7 +223,7 @@ def extra_adjoint(up, W, stream):
     planet = up.Planet(program=P)
     planet.set_stream(stream.cuda_stream)
     n = 1 << 24
-    x = _shell(planet, n, 0.05, seed=11)
+    x = _morton_sorted(_shell(planet, n, 0.05, seed=11))
     v = torch.empty(n, device="cuda")
     g = torch.empty((n, 3), device="cuda")
     nt = W.theta_count(P)
@@ -221,7 +236,7 @@ def extra_adjoint(up, W, stream):
     f_ms, b_ms = _events(stream, fwd, 5), _events(stream, bwd, 5)
     return {"points": n, "theta": nt, "forward_ms": f_ms, "backward_ms": b_ms, "backward_gpoints_s": n / b_ms / 1e6,
             "what": "torus + 8 spheres - ridged perlin + cellular; forward value+dd/dp, backward dL/dtheta of mean(d^2) "
-                    "over the 25 parameters, 16M points uniform in the 0.05 shell"}
+                    "over the 25 parameters, 16M points uniform in the 0.05 shell (Morton order, sorted once when generated)"}
 
 
 def extra_batch(up, W, stream):
@@ -286,7 +301,7 @@ def extra_fit(up, W, stream, steps=300):
     target.set_stream(stream.cuda_stream)
     target.set_theta(t_star_np)
     n = 32 << 20
-    x = _shell(target, n, 0.05, seed=21)
+    x = _morton_sorted(_shell(target, n, 0.05, seed=21))
     gg = W.grid(W.GRID_C2, n=(256, 256, 256))
     xg = AG.grid_positions(gg)  # the grid kernel's sample positions
     d_star = target.sdf_points(x, d=torch.empty(n, device="cuda"))
@@ -332,7 +347,7 @@ def extra_fit(up, W, stream, steps=300):
             "theta_rel_err_by_group_start": group_err(t0), "theta_rel_err_by_group_end": group_err(theta.detach().cpu().numpy()),
             "sdf_rms_vs_fp64_oracle": float(np.sqrt(np.mean((fit - ref) ** 2))),
             "what": "torus + 8 spheres - ridged perlin + cellular, 25 parameters; theta* = theta (1 + 0.05 U) seed 1, "
-                    "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell + "
+                    "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell (Morton order) + "
                     "mean(relu(-d sign(d*))) on 256^3 (forward through the grid kernel); Adam lr 1e-2; SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
 
 
