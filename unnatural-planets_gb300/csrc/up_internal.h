@@ -20,14 +20,16 @@ struct ModesDesc;
 
 // ---- SDF sampling (up_sdf.cu / up_modes.cu)
 // band > 0: narrow band of contouring (samples with |base| > band keep the
-// base value); 0: exact values everywhere
-cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s,
+// base value); 0: exact values everywhere. flags: two device words, [0] the
+// NaN flag (set, never cleared, by the kernel), [1] the task counter of the
+// x-coherent grid kernels (zeroed by the launcher, in stream order).
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s,
 	float band = 0.f);
 // narrow band of contouring for program P on grid g (0 when unbounded)
 float contour_band(const up_synth_program &P, const GridDev &g);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 // band > 0: narrow band of contouring one field (modes_contour_band)
-cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &host, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *nanflag,
+cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &host, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *flags,
 	cudaStream_t s, float band = 0.f);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 

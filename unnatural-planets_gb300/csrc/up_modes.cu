@@ -71,7 +71,8 @@ constexpr int MRUN_SLOTS = 4; // slots 0-2: noise instances, then the three fiel
 
 template<int EM>
 __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g,
-	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, unsigned *__restrict__ nanflag, float band) {
+	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks,
+	float band) {
 	extern __shared__ __align__(16) float mruns_smem[];
 	constexpr int R = RUN_R;
 	float *tab = mruns_smem + threadIdx.x;
@@ -81,10 +82,10 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 	const uint32_t nruns = (nx + R - 1) / R;
 	const uint32_t tny = (ny + 7) / 8, tnz = (nz + 3) / 4;
 	// a task holds at least two samples of a grid of 2 .. 2^32 - 1 samples:
-	// ntasks < 2^31, and t + nwarps below cannot wrap
+	// ntasks < 2^31, and the counter (ntasks plus one failed take per warp)
+	// cannot wrap
 	const uint32_t ntasks = nruns * tny * tnz;
 	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
 	const bool need_e = (mask & 5u) != 0;
 	float *const outs[3] = {o0, o1, o2};
 	runs_tables_init();
@@ -93,7 +94,13 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 	rc.step_x = g.step[0];
 	rc.nx = nx;
 	bool bad = false;
-	for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nwarps) {
+	// tasks in order from the launcher-zeroed counter (synth_grid_runs_kernel)
+	uint32_t t = 0;
+	if (lane == 0) t = atomicAdd(tasks, 1u);
+	t = __shfl_sync(0xFFFFFFFFu, t, 0);
+	while (t < ntasks) {
+		uint32_t t_next = 0;
+		if (lane == 0) t_next = atomicAdd(tasks, 1u); // taken ahead; read after the task
 		const uint32_t run = t % nruns, tile = t / nruns;
 		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
 		const bool live = jr < ny && kr < nz;
@@ -112,33 +119,35 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 			#pragma unroll
 			for (int f = 0; f < 3; f++) tab[(f * R + r) * MRUNS_T] = v[f];
 		}
-		if (!live) continue;
-		const uint64_t base = ((uint64_t)k * ny + j) * nx + rc.i0;
-		const bool full = rc.i0 + R <= nx;
-		#pragma unroll 1
-		for (int f = 0; f < 3; f++) {
-			if (!(mask & (1u << f))) continue;
-			float *o = outs[f];
-			const float *src = tab + f * R * MRUNS_T;
-			// 16-byte stores only where the destination is 16-byte aligned
-			const bool vec = full && ((uintptr_t)(o + base) & 15) == 0;
+		if (live) {
+			const uint64_t base = ((uint64_t)k * ny + j) * nx + rc.i0;
+			const bool full = rc.i0 + R <= nx;
 			#pragma unroll 1
-			for (int r = 0; r < R; r += 4) {
-				float x[4];
-				#pragma unroll
-				for (int q = 0; q < 4; q++) {
-					x[q] = src[(r + q) * MRUNS_T];
-					bad |= isnan(x[q]);
-				}
-				if (vec) {
-					*(float4 *)(o + base + r) = make_float4(x[0], x[1], x[2], x[3]);
-				} else {
+			for (int f = 0; f < 3; f++) {
+				if (!(mask & (1u << f))) continue;
+				float *o = outs[f];
+				const float *src = tab + f * R * MRUNS_T;
+				// 16-byte stores only where the destination is 16-byte aligned
+				const bool vec = full && ((uintptr_t)(o + base) & 15) == 0;
+				#pragma unroll 1
+				for (int r = 0; r < R; r += 4) {
+					float x[4];
 					#pragma unroll
-					for (int q = 0; q < 4; q++)
-						if (rc.i0 + r + q < nx) o[base + r + q] = x[q];
+					for (int q = 0; q < 4; q++) {
+						x[q] = src[(r + q) * MRUNS_T];
+						bad |= isnan(x[q]);
+					}
+					if (vec) {
+						*(float4 *)(o + base + r) = make_float4(x[0], x[1], x[2], x[3]);
+					} else {
+						#pragma unroll
+						for (int q = 0; q < 4; q++)
+							if (rc.i0 + r + q < nx) o[base + r + q] = x[q];
+					}
 				}
 			}
 		}
+		t = __shfl_sync(0xFFFFFFFFu, t_next, 0);
 	}
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
 }
@@ -176,28 +185,31 @@ static cudaError_t launch_p(K kernel, uint64_t work, cudaStream_t s, A... args) 
 	return cudaGetLastError();
 }
 
+// tasks: the kernel's task counter, zeroed here in stream order
 template<class K, class... A>
-static cudaError_t launch_mruns(K kernel, const GridDev &g, cudaStream_t s, A... args) {
+static cudaError_t launch_mruns(K kernel, const GridDev &g, cudaStream_t s, unsigned *tasks, A... args) {
 	constexpr size_t smem = (size_t)MRUN_SLOTS * RUN_R * MRUNS_T * sizeof(float); // 64 KiB
-	const cudaError_t e = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
+	if ((e = cudaMemsetAsync(tasks, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
 	uint64_t blocks = (uint64_t)persistent_blocks((const void *)kernel, MRUNS_T, smem);
-	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
-	const uint64_t need = (tasks + MRUNS_T / 32 - 1) / (MRUNS_T / 32);
+	const uint64_t ntasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
+	const uint64_t need = (ntasks + MRUNS_T / 32 - 1) / (MRUNS_T / 32);
 	if (blocks > need) blocks = need > 0 ? need : 1;
 	kernel<<<(unsigned)blocks, MRUNS_T, smem, s>>>(args...);
 	return cudaGetLastError();
 }
 
 cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &H, uint32_t mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
-	unsigned *nanflag, cudaStream_t s, float band) {
+	unsigned *flags, cudaStream_t s, float band) {
+	unsigned *const nanflag = flags, *const tasks = flags + 1;
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
 	if (grad) return launch_p(modes_grid_kernel<true>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, 0.f);
 	if ((mask & 5u) && mrun_applies(H)) {
-		if (H.elevation == 2) return launch_mruns(modes_grid_runs_kernel<2>, g, s, M, mask, g, o0, o1, o2, nanflag, band);
-		if (H.elevation == 3) return launch_mruns(modes_grid_runs_kernel<3>, g, s, M, mask, g, o0, o1, o2, nanflag, band);
-		return launch_mruns(modes_grid_runs_kernel<4>, g, s, M, mask, g, o0, o1, o2, nanflag, band);
+		if (H.elevation == 2) return launch_mruns(modes_grid_runs_kernel<2>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band);
+		if (H.elevation == 3) return launch_mruns(modes_grid_runs_kernel<3>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band);
+		return launch_mruns(modes_grid_runs_kernel<4>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band);
 	}
 	return launch_p(modes_grid_kernel<false>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, band);
 }

@@ -81,7 +81,7 @@ static_assert(RUNS_T == 32 * RUNS_WARPS, "the x tables of up_grid_runs.cuh hold 
 // blocks (5 per SM, shared-memory bound: 5.25 ms at 512^3) and 2-warp blocks.
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
-	float *__restrict__ grad, unsigned *__restrict__ nanflag, float band) {
+	float *__restrict__ grad, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks, float band) {
 	typedef typename AccOf<GRAD>::T A;
 	extern __shared__ __align__(16) unsigned char runs_smem[];
 	A *acc = (A *)runs_smem + threadIdx.x;
@@ -92,18 +92,27 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 	const uint32_t nruns = (nx + R - 1) / R;
 	const uint32_t tny = (ny + 7) / 8, tnz = (nz + 3) / 4;
 	// a task holds at least two samples of a grid of 2 .. 2^32 - 1 samples:
-	// ntasks < 2^31, and t + nwarps below cannot wrap
+	// ntasks < 2^31, and the counter (ntasks plus one failed take per warp)
+	// cannot wrap
 	const uint32_t ntasks = nruns * tny * tnz;
 	const uint64_t plane = (uint64_t)nx * nrows;
 	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
 	runs_tables_init();
 	RunCtx rc;
 	rc.lo_x = g.lo[0];
 	rc.step_x = g.step[0];
 	rc.nx = nx;
 	bool bad = false;
-	for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nwarps) {
+	// Warps take tasks in order from a counter that the launcher zeroes: task
+	// costs differ (under the narrow band a task near the surface evaluates
+	// the noise and one far from it stores the base), and a fixed
+	// assignment of every nwarps-th task left some warps twice the mean work.
+	uint32_t t = 0;
+	if (lane == 0) t = atomicAdd(tasks, 1u);
+	t = __shfl_sync(0xFFFFFFFFu, t, 0);
+	while (t < ntasks) {
+		uint32_t t_next = 0;
+		if (lane == 0) t_next = atomicAdd(tasks, 1u); // taken ahead; read after the task
 		const uint32_t run = t % nruns, tile = t / nruns;
 		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
 		const bool live = jr < ny && kr < nz;
@@ -113,50 +122,52 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 		rc.py = grid_coord(g, 1, j);
 		rc.pz = grid_coord(g, 2, k + g.k0);
 		synth_run<GRAD, T0, T1>(P, rc, R, acc, RUNS_T, band);
-		if (!live) continue;
-		const uint64_t base = (uint64_t)row * nx + rc.i0;
-		// 16-byte stores only where every destination address is 16-byte
-		// aligned (caller pointers and plane offsets need not be)
-		const bool full = rc.i0 + R <= nx;
-		const bool vec = full && ((uintptr_t)(out + base) & 15) == 0;
-		const bool vecg = GRAD && full &&
-			(((uintptr_t)(grad + base) | (uintptr_t)(grad + plane + base) | (uintptr_t)(grad + 2 * plane + base)) & 15) == 0;
-		#pragma unroll 1
-		for (int r = 0; r < R; r += 4) {
-			float v[4], gx[4], gy[4], gz[4];
-			#pragma unroll
-			for (int q = 0; q < 4; q++) {
-				if (GRAD) {
-					const Acc4 x = ((const Acc4 *)acc)[(r + q) * RUNS_T];
-					v[q] = x.v; gx[q] = x.gx; gy[q] = x.gy; gz[q] = x.gz;
-				} else {
-					v[q] = ((const float *)acc)[(r + q) * RUNS_T];
-				}
-				bad |= isnan(v[q]);
-			}
-			if (vec) {
-				*(float4 *)(out + base + r) = make_float4(v[0], v[1], v[2], v[3]);
-			} else {
+		if (live) {
+			const uint64_t base = (uint64_t)row * nx + rc.i0;
+			// 16-byte stores only where every destination address is 16-byte
+			// aligned (caller pointers and plane offsets need not be)
+			const bool full = rc.i0 + R <= nx;
+			const bool vec = full && ((uintptr_t)(out + base) & 15) == 0;
+			const bool vecg = GRAD && full &&
+				(((uintptr_t)(grad + base) | (uintptr_t)(grad + plane + base) | (uintptr_t)(grad + 2 * plane + base)) & 15) == 0;
+			#pragma unroll 1
+			for (int r = 0; r < R; r += 4) {
+				float v[4], gx[4], gy[4], gz[4];
 				#pragma unroll
-				for (int q = 0; q < 4; q++)
-					if (rc.i0 + r + q < nx) out[base + r + q] = v[q];
-			}
-			if (GRAD) {
-				if (vecg) {
-					*(float4 *)(grad + base + r) = make_float4(gx[0], gx[1], gx[2], gx[3]);
-					*(float4 *)(grad + plane + base + r) = make_float4(gy[0], gy[1], gy[2], gy[3]);
-					*(float4 *)(grad + 2 * plane + base + r) = make_float4(gz[0], gz[1], gz[2], gz[3]);
+				for (int q = 0; q < 4; q++) {
+					if (GRAD) {
+						const Acc4 x = ((const Acc4 *)acc)[(r + q) * RUNS_T];
+						v[q] = x.v; gx[q] = x.gx; gy[q] = x.gy; gz[q] = x.gz;
+					} else {
+						v[q] = ((const float *)acc)[(r + q) * RUNS_T];
+					}
+					bad |= isnan(v[q]);
+				}
+				if (vec) {
+					*(float4 *)(out + base + r) = make_float4(v[0], v[1], v[2], v[3]);
 				} else {
 					#pragma unroll
 					for (int q = 0; q < 4; q++)
-						if (rc.i0 + r + q < nx) {
-							grad[base + r + q] = gx[q];
-							grad[plane + base + r + q] = gy[q];
-							grad[2 * plane + base + r + q] = gz[q];
-						}
+						if (rc.i0 + r + q < nx) out[base + r + q] = v[q];
+				}
+				if (GRAD) {
+					if (vecg) {
+						*(float4 *)(grad + base + r) = make_float4(gx[0], gx[1], gx[2], gx[3]);
+						*(float4 *)(grad + plane + base + r) = make_float4(gy[0], gy[1], gy[2], gy[3]);
+						*(float4 *)(grad + 2 * plane + base + r) = make_float4(gz[0], gz[1], gz[2], gz[3]);
+					} else {
+						#pragma unroll
+						for (int q = 0; q < 4; q++)
+							if (rc.i0 + r + q < nx) {
+								grad[base + r + q] = gx[q];
+								grad[plane + base + r + q] = gy[q];
+								grad[2 * plane + base + r + q] = gz[q];
+							}
+					}
 				}
 			}
 		}
+		t = __shfl_sync(0xFFFFFFFFu, t_next, 0);
 	}
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
 }
@@ -199,15 +210,17 @@ static cudaError_t launch_persistent(K kernel, uint64_t work, cudaStream_t s, A.
 	return cudaGetLastError();
 }
 
+// tasks: the kernel's task counter, zeroed here in stream order
 template<bool GRAD, class K, class... A>
-static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, A... args) {
+static cudaError_t launch_runs(K kernel, const GridDev &g, cudaStream_t s, unsigned *tasks, A... args) {
 	// 64 KiB (value + gradient) or 16 KiB of accumulators
 	constexpr size_t smem = (size_t)RUN_R * RUNS_T * sizeof(typename AccOf<GRAD>::T);
-	const cudaError_t e = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
+	if ((e = cudaMemsetAsync(tasks, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
 	uint64_t blocks = (uint64_t)persistent_blocks((const void *)kernel, RUNS_T, smem);
-	const uint64_t tasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
-	const uint64_t need = (tasks + RUNS_T / 32 - 1) / (RUNS_T / 32);
+	const uint64_t ntasks = (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
+	const uint64_t need = (ntasks + RUNS_T / 32 - 1) / (RUNS_T / 32);
 	if (blocks > need) blocks = need > 0 ? need : 1;
 	kernel<<<(unsigned)blocks, RUNS_T, smem, s>>>(args...);
 	return cudaGetLastError();
@@ -228,13 +241,14 @@ float contour_band(const up_synth_program &P, const GridDev &g) {
 	const float band = (B + st) * 1.001f + 1e-5f;
 	return std::isfinite(band) ? band : 0.f;
 }
-cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *nanflag, cudaStream_t s, float band) {
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s, float band) {
+	unsigned *const nanflag = flags, *const tasks = flags + 1;
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
 	const Spec sp = spec_of(P);
 	if (sp == SPEC_PERLIN_CELL) {
-		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag, band);
-		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, P, g, out, grad, nanflag, band);
+		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band);
+		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band);
 	}
 	if (grad) {
 		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag, band);
