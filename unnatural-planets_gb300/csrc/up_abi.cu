@@ -36,7 +36,7 @@ using namespace up;
 
 enum BufSlot {
 	B_IN0, B_OUT0, B_OUT1, B_OUT2, B_GRAD, B_GRID, B_PARTIALS, B_W,
-	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS, B_DC_FB, B_DC_FBF,
+	B_DC_BLK, B_DC_TOT, B_DC_CMAP, B_DC_EMAP, B_DC_CLIST, B_DC_ELIST, B_DC_QLIST, B_DC_ET, B_DC_EN, B_DC_SIGNS, B_DC_FB, B_DC_FBF, B_TASKL,
 	B_MESH_POS, B_MESH_NRM, B_MESH_IDX,
 	B_TEX0, B_TEX1, B_TEX2, B_TEX3, B_TEX4, B_TEX5, B_TEX6, B_TEX7, B_TEX8, B_TEX9, B_TEXIA,
 	B_BATCH0, B_BATCH1, B_BATCH2, B_BATCH3, B_BATCH4, B_BATCH5, B_BATCH6, B_BATCH7,
@@ -223,8 +223,10 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 	} else {
 		float *gd = (float *)buf(ctx, B_GRID, np * 4);
 		reset_flag(ctx);
-		if (ctx->synthetic) check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream, contour_band(ctx->prog, c.g)), "sdf grid kernel");
-		else {
+		if (ctx->synthetic) {
+			uint32_t *tl = (uint32_t *)buf(ctx, B_TASKL, runs_task_count(c.g) * 4);
+			check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream, contour_band(ctx->prog, c.g), tl), "sdf grid kernel");
+		} else {
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;
 			check(launch_modes_grid(ctx->d_modes, ctx->modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream,

@@ -20,11 +20,16 @@ struct ModesDesc;
 
 // ---- SDF sampling (up_sdf.cu / up_modes.cu)
 // band > 0: narrow band of contouring (samples with |base| > band keep the
-// base value); 0: exact values everywhere. flags: two device words, [0] the
-// NaN flag (set, never cleared, by the kernel), [1] the task counter of the
-// x-coherent grid kernels (zeroed by the launcher, in stream order).
+// base value); 0: exact values everywhere. flags: three device words, [0]
+// the NaN flag (set, never cleared, by the kernel), [1] the task counter of
+// the x-coherent grid kernels and [2] their count of listed tasks (both
+// zeroed by the launcher, in stream order). task_list (runs_task_count
+// words, or null): lets a narrow-band value launch sample only the tasks
+// near the surface; the others get one value of the right sign per task.
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s,
-	float band = 0.f);
+	float band = 0.f, uint32_t *task_list = nullptr);
+// work units (tasks) of the x-coherent grid kernels on grid g
+uint64_t runs_task_count(const GridDev &g);
 // narrow band of contouring for program P on grid g (0 when unbounded)
 float contour_band(const up_synth_program &P, const GridDev &g);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);

@@ -79,9 +79,12 @@ static_assert(RUNS_T == 32 * RUNS_WARPS, "the x tables of up_grid_runs.cuh hold 
 // (64 KiB of accumulators plus 10 KiB of tables per block) admits 3, and the
 // cap keeps the registers (80) from admitting fewer. Timed against 4-warp
 // blocks (5 per SM, shared-memory bound: 5.25 ms at 512^3) and 2-warp blocks.
+// task_list (narrow band only, or null): the tasks to sample, *list_count of
+// them, listed by synth_task_band_kernel, which has written the others.
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
-	float *__restrict__ grad, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks, float band) {
+	float *__restrict__ grad, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks, float band,
+	const uint32_t *__restrict__ task_list, const unsigned *__restrict__ list_count) {
 	typedef typename AccOf<GRAD>::T A;
 	extern __shared__ __align__(16) unsigned char runs_smem[];
 	A *acc = (A *)runs_smem + threadIdx.x;
@@ -94,7 +97,7 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 	// a task holds at least two samples of a grid of 2 .. 2^32 - 1 samples:
 	// ntasks < 2^31, and the counter (ntasks plus one failed take per warp)
 	// cannot wrap
-	const uint32_t ntasks = nruns * tny * tnz;
+	const uint32_t ntasks = task_list ? *list_count : nruns * tny * tnz;
 	const uint64_t plane = (uint64_t)nx * nrows;
 	const uint32_t lane = threadIdx.x & 31;
 	runs_tables_init();
@@ -113,7 +116,8 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 	while (t < ntasks) {
 		uint32_t t_next = 0;
 		if (lane == 0) t_next = atomicAdd(tasks, 1u); // taken ahead; read after the task
-		const uint32_t run = t % nruns, tile = t / nruns;
+		const uint32_t tt = task_list ? task_list[t] : t;
+		const uint32_t run = tt % nruns, tile = tt / nruns;
 		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
 		const bool live = jr < ny && kr < nz;
 		const uint32_t j = jr < ny ? jr : ny - 1, k = kr < nz ? kr : nz - 1;
@@ -170,6 +174,70 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 		t = __shfl_sync(0xFFFFFFFFu, t_next, 0);
 	}
 	if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(nanflag, 1u);
+}
+
+// Narrow band at the task level (a task: RUN_R samples along x of 8 x 4
+// rows, the work unit of synth_grid_runs_kernel). The base is 1-Lipschitz, so
+// a task whose sample box lies farther from the base's surface than the band
+// (|base(centre)| above band plus the box's half diagonal; margins as in
+// synth_run) holds no sample with |base| <= band, and base(centre) has the
+// sign of every one of its samples. This kernel writes that value to every
+// sample of such tasks and lists the other tasks (order unspecified) for the
+// runs kernel: lane i of a warp tests task 32 w + i, then the warp stores the
+// far tasks of its 32 one after the other, a task's 32 rows of 16 samples as
+// 128 16-byte pieces, 8 whole rows per store instruction (with a lane per
+// row, each store instruction half-filled 32 sectors: 2.9x slower).
+__global__ void __launch_bounds__(256) synth_task_band_kernel(const up_synth_program P, const GridDev g, float band, float *__restrict__ out,
+	uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count) {
+	constexpr uint32_t R = RUN_R;
+	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const uint32_t nruns = (nx + R - 1) / R, tny = (ny + 7) / 8, tnz = (nz + 3) / 4;
+	const uint32_t ntasks = nruns * tny * tnz; // < 2^31 (synth_grid_runs_kernel)
+	const uint32_t ngroups = (ntasks + 31) / 32;
+	const uint32_t lane = threadIdx.x & 31;
+	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ngroups; w += (gridDim.x * blockDim.x) >> 5) {
+		const uint32_t t = w * 32 + lane;
+		bool far = false;
+		float fv = 0.f;
+		if (t < ntasks) {
+			const uint32_t run = t % nruns, tile = t / nruns;
+			const uint32_t i0 = run * R, j0 = (tile % tny) * 8, k0 = (tile / tny) * 4;
+			const uint32_t i1 = min(i0 + R - 1, nx - 1), j1 = min(j0 + 7, ny - 1), k1 = min(k0 + 3, nz - 1);
+			const float x0 = grid_coord(g, 0, i0), x1 = grid_coord(g, 0, i1);
+			const float y0 = grid_coord(g, 1, j0), y1 = grid_coord(g, 1, j1);
+			const float z0 = grid_coord(g, 2, k0 + g.k0), z1 = grid_coord(g, 2, k1 + g.k0);
+			const V3f c = v3(0.5f * (x0 + x1), 0.5f * (y0 + y1), 0.5f * (z0 + z1));
+			const V3f h = v3(0.5f * fabsf(x1 - x0), 0.5f * fabsf(y1 - y0), 0.5f * fabsf(z1 - z0));
+			fv = synth_base<false>(P, c).v;
+			far = fabsf(fv) > (band + sqrtf(dot(h, h))) * 1.001f + 1e-5f; // false for NaN
+		}
+		const unsigned near = __ballot_sync(0xFFFFFFFFu, t < ntasks && !far);
+		uint32_t slot = 0;
+		if (lane == 0 && near) slot = atomicAdd(list_count, (unsigned)__popc(near));
+		slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+		if (near & (1u << lane)) task_list[slot + __popc(near & ((1u << lane) - 1u))] = t;
+		#pragma unroll 1
+		for (unsigned fm = __ballot_sync(0xFFFFFFFFu, far); fm != 0u; fm &= fm - 1u) {
+			const int src = __ffs(fm) - 1;
+			const float v = __shfl_sync(0xFFFFFFFFu, fv, src);
+			const uint32_t tf = w * 32 + (uint32_t)src;
+			const uint32_t run = tf % nruns, tile = tf / nruns;
+			const uint32_t i0 = run * R, j0 = (tile % tny) * 8, k0 = (tile / tny) * 4;
+			#pragma unroll
+			for (uint32_t q = 0; q < 4; q++) {
+				const uint32_t piece = q * 32 + lane, rr = piece >> 2, x = i0 + (piece & 3) * 4;
+				const uint32_t jr = j0 + (rr & 7), kr = k0 + (rr >> 3);
+				if (jr >= ny || kr >= nz || x >= nx) continue;
+				float *o = out + ((uint64_t)kr * ny + jr) * nx + x;
+				if (x + 4 <= nx && ((uintptr_t)o & 15) == 0) {
+					*(float4 *)o = make_float4(v, v, v, v);
+				} else {
+					#pragma unroll 1
+					for (uint32_t r = 0; r < 4 && x + r < nx; r++) o[r] = v;
+				}
+			}
+		}
+	}
 }
 
 // Every lane of a warp runs every step (lanes past n evaluate the last point
@@ -241,14 +309,31 @@ float contour_band(const up_synth_program &P, const GridDev &g) {
 	const float band = (B + st) * 1.001f + 1e-5f;
 	return std::isfinite(band) ? band : 0.f;
 }
-cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s, float band) {
-	unsigned *const nanflag = flags, *const tasks = flags + 1;
+uint64_t runs_task_count(const GridDev &g) {
+	return (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
+}
+cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s, float band,
+	uint32_t *task_list) {
+	unsigned *const nanflag = flags, *const tasks = flags + 1, *const list_count = flags + 2;
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
 	const Spec sp = spec_of(P);
 	if (sp == SPEC_PERLIN_CELL) {
-		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band);
-		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band);
+		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band,
+			(const uint32_t *)nullptr, (const unsigned *)nullptr);
+		if (band > 0.f && task_list) {
+			cudaError_t e = cudaMemsetAsync(list_count, 0, sizeof(unsigned), s);
+			if (e != cudaSuccess) return e;
+			const uint64_t groups = (runs_task_count(g) + 31) / 32;
+			uint64_t blocks = (uint64_t)persistent_blocks((const void *)synth_task_band_kernel, 256);
+			if (blocks > (groups + 7) / 8) blocks = (groups + 7) / 8;
+			synth_task_band_kernel<<<(unsigned)blocks, 256, 0, s>>>(P, g, band, out, task_list, list_count);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band,
+				(const uint32_t *)task_list, (const unsigned *)list_count);
+		}
+		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band,
+			(const uint32_t *)nullptr, (const unsigned *)nullptr);
 	}
 	if (grad) {
 		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag, band);
