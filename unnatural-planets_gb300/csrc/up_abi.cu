@@ -229,8 +229,9 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 		} else {
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;
+			uint32_t *tl = (uint32_t *)buf(ctx, B_TASKL, runs_task_count(c.g) * 4);
 			check(launch_modes_grid(ctx->d_modes, ctx->modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream,
-				modes_contour_band(ctx->modes, field, c.g.step)), "sdf grid kernel");
+				modes_contour_band(ctx->modes, field, c.g.step), tl), "sdf grid kernel");
 		}
 		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
 		c.d = gd;

@@ -404,6 +404,59 @@ UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename 
 	}
 }
 
+#ifdef __CUDACC__
+// Sample box of task t of the x-coherent grid kernels (below) on grid g
+// (fields n, lo, step, k0 of GridDev; coordinates as the kernels form them):
+// its centre c and half diagonal hd.
+template<class G>
+__device__ __forceinline__ void runs_task_box(const G &g, uint32_t t, V3f &c, float &hd) {
+	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const uint32_t nruns = (nx + RUN_R - 1) / RUN_R, tny = (ny + 7) / 8;
+	const uint32_t run = t % nruns, tile = t / nruns;
+	const uint32_t lo[3] = {run * RUN_R, (tile % tny) * 8, (tile / tny) * 4};
+	const uint32_t hi[3] = {min(lo[0] + RUN_R - 1, nx - 1), min(lo[1] + 7, ny - 1), min(lo[2] + 3, nz - 1)};
+	float cc[3], h2 = 0.f;
+	#pragma unroll
+	for (int a = 0; a < 3; a++) {
+		const uint32_t off = a == 2 ? g.k0 : 0u;
+		const float x0 = __fadd_rn(__fmul_rn((float)(lo[a] + off), g.step[a]), g.lo[a]);
+		const float x1 = __fadd_rn(__fmul_rn((float)(hi[a] + off), g.step[a]), g.lo[a]);
+		const float h = 0.5f * fabsf(x1 - x0);
+		cc[a] = 0.5f * (x0 + x1);
+		h2 += h * h;
+	}
+	c = v3(cc[0], cc[1], cc[2]);
+	hd = sqrtf(h2);
+}
+
+// Task t of the x-coherent grid kernels (RUN_R samples along x of an 8 (y) x
+// 4 (z) tile of rows; tasks numbered x-run fastest) of an nx x ny x nz grid:
+// stores v at every sample, warp-wide (every lane calls it with the same t
+// and v). The task's 32 rows of RUN_R samples go out as 128 16-byte pieces,
+// 8 whole rows per store instruction (with a lane per row, each store
+// instruction half-filled 32 sectors: 2.9x slower).
+__device__ __forceinline__ void runs_task_fill(float *__restrict__ out, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t t, float v) {
+	static_assert(RUN_R == 16, "four 16-byte pieces per row");
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t nruns = (nx + RUN_R - 1) / RUN_R, tny = (ny + 7) / 8;
+	const uint32_t run = t % nruns, tile = t / nruns;
+	const uint32_t i0 = run * RUN_R, j0 = (tile % tny) * 8, k0 = (tile / tny) * 4;
+	#pragma unroll
+	for (uint32_t q = 0; q < 4; q++) {
+		const uint32_t piece = q * 32 + lane, rr = piece >> 2, x = i0 + (piece & 3) * 4;
+		const uint32_t jr = j0 + (rr & 7), kr = k0 + (rr >> 3);
+		if (jr >= ny || kr >= nz || x >= nx) continue;
+		float *o = out + ((uint64_t)kr * ny + jr) * nx + x;
+		if (x + 4 <= nx && ((uintptr_t)o & 15) == 0) {
+			*(float4 *)o = make_float4(v, v, v, v);
+		} else {
+			#pragma unroll 1
+			for (uint32_t r = 0; r < 4 && x + r < nx; r++) o[r] = v;
+		}
+	}
+}
+#endif
+
 // one run: base shape plus layers into acc (R must be a multiple of CELL_SUB).
 // band > 0 (narrow band of contouring, values only): when every sample of the
 // warp's task has |base| > band, the layers are skipped and acc holds the

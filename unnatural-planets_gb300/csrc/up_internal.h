@@ -35,7 +35,7 @@ float contour_band(const up_synth_program &P, const GridDev &g);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 // band > 0: narrow band of contouring one field (modes_contour_band)
 cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &host, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *flags,
-	cudaStream_t s, float band = 0.f);
+	cudaStream_t s, float band = 0.f, uint32_t *task_list = nullptr);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 
 // adjoint: partial sums per block into partials (nblocks x ACC stride), then

@@ -69,10 +69,51 @@ __global__ void __launch_bounds__(128) modes_grid_kernel(const ModesDesc *__rest
 constexpr int MRUNS_T = 32 * RUNS_WARPS;
 constexpr int MRUN_SLOTS = 4; // slots 0-2: noise instances, then the three fields (in place); 3: shape values
 
+// Narrow band at the task level (synth_task_band_kernel, with the shape as
+// the base and the margin of modes_run_shape): tasks whose sample box lies
+// farther than the band from the shape's surface get shape(centre) in every
+// selected field; the others are listed for modes_grid_runs_kernel.
+__global__ void __launch_bounds__(256) modes_task_band_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g, float band,
+	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count) {
+	const ModesDesc &M = *Mp;
+	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const uint32_t ntasks = ((nx + RUN_R - 1) / RUN_R) * ((ny + 7) / 8) * ((nz + 3) / 4); // < 2^31
+	const uint32_t ngroups = (ntasks + 31) / 32;
+	const uint32_t lane = threadIdx.x & 31;
+	float *const outs[3] = {o0, o1, o2};
+	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ngroups; w += (gridDim.x * blockDim.x) >> 5) {
+		const uint32_t t = w * 32 + lane;
+		bool far = false;
+		float fv = 0.f;
+		if (t < ntasks) {
+			V3f c;
+			float hd;
+			runs_task_box(g, t, c, hd);
+			fv = shape_eval(M, vs(c.x, c.y, c.z));
+			far = fabsf(fv) > (band + hd) * 1.001f + 1e-3f * (1.f + fabsf(fv)); // false for NaN
+		}
+		const unsigned near = __ballot_sync(0xFFFFFFFFu, t < ntasks && !far);
+		uint32_t slot = 0;
+		if (lane == 0 && near) slot = atomicAdd(list_count, (unsigned)__popc(near));
+		slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+		if (near & (1u << lane)) task_list[slot + __popc(near & ((1u << lane) - 1u))] = t;
+		#pragma unroll 1
+		for (unsigned fm = __ballot_sync(0xFFFFFFFFu, far); fm != 0u; fm &= fm - 1u) {
+			const int src = __ffs(fm) - 1;
+			const float v = __shfl_sync(0xFFFFFFFFu, fv, src);
+			#pragma unroll 1
+			for (int f = 0; f < 3; f++)
+				if (mask & (1u << f)) runs_task_fill(outs[f], nx, ny, nz, w * 32 + (uint32_t)src, v);
+		}
+	}
+}
+
+// task_list (narrow band only, or null): the tasks to sample, *list_count of
+// them, listed by modes_task_band_kernel, which has written the others.
 template<int EM>
 __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g,
 	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks,
-	float band) {
+	float band, const uint32_t *__restrict__ task_list, const unsigned *__restrict__ list_count) {
 	extern __shared__ __align__(16) float mruns_smem[];
 	constexpr int R = RUN_R;
 	float *tab = mruns_smem + threadIdx.x;
@@ -84,7 +125,7 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 	// a task holds at least two samples of a grid of 2 .. 2^32 - 1 samples:
 	// ntasks < 2^31, and the counter (ntasks plus one failed take per warp)
 	// cannot wrap
-	const uint32_t ntasks = nruns * tny * tnz;
+	const uint32_t ntasks = task_list ? *list_count : nruns * tny * tnz;
 	const uint32_t lane = threadIdx.x & 31;
 	const bool need_e = (mask & 5u) != 0;
 	float *const outs[3] = {o0, o1, o2};
@@ -101,7 +142,8 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 	while (t < ntasks) {
 		uint32_t t_next = 0;
 		if (lane == 0) t_next = atomicAdd(tasks, 1u); // taken ahead; read after the task
-		const uint32_t run = t % nruns, tile = t / nruns;
+		const uint32_t tt = task_list ? task_list[t] : t;
+		const uint32_t run = tt % nruns, tile = tt / nruns;
 		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
 		const bool live = jr < ny && kr < nz;
 		const uint32_t j = jr < ny ? jr : ny - 1, k = kr < nz ? kr : nz - 1;
@@ -201,15 +243,28 @@ static cudaError_t launch_mruns(K kernel, const GridDev &g, cudaStream_t s, unsi
 }
 
 cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &H, uint32_t mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
-	unsigned *flags, cudaStream_t s, float band) {
-	unsigned *const nanflag = flags, *const tasks = flags + 1;
+	unsigned *flags, cudaStream_t s, float band, uint32_t *task_list) {
+	unsigned *const nanflag = flags, *const tasks = flags + 1, *const list_count = flags + 2;
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
 	if (grad) return launch_p(modes_grid_kernel<true>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, 0.f);
 	if ((mask & 5u) && mrun_applies(H)) {
-		if (H.elevation == 2) return launch_mruns(modes_grid_runs_kernel<2>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band);
-		if (H.elevation == 3) return launch_mruns(modes_grid_runs_kernel<3>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band);
-		return launch_mruns(modes_grid_runs_kernel<4>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band);
+		const uint32_t *tl = nullptr;
+		const unsigned *tc = nullptr;
+		if (band > 0.f && task_list) {
+			cudaError_t e = cudaMemsetAsync(list_count, 0, sizeof(unsigned), s);
+			if (e != cudaSuccess) return e;
+			const uint64_t groups = (runs_task_count(g) + 31) / 32;
+			uint64_t blocks = (uint64_t)persistent_blocks((const void *)modes_task_band_kernel, 256);
+			if (blocks > (groups + 7) / 8) blocks = (groups + 7) / 8;
+			modes_task_band_kernel<<<(unsigned)blocks, 256, 0, s>>>(M, mask, g, band, o0, o1, o2, task_list, list_count);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			tl = task_list;
+			tc = list_count;
+		}
+		if (H.elevation == 2) return launch_mruns(modes_grid_runs_kernel<2>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc);
+		if (H.elevation == 3) return launch_mruns(modes_grid_runs_kernel<3>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc);
+		return launch_mruns(modes_grid_runs_kernel<4>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc);
 	}
 	return launch_p(modes_grid_kernel<false>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, band);
 }

@@ -184,15 +184,11 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 // sign of every one of its samples. This kernel writes that value to every
 // sample of such tasks and lists the other tasks (order unspecified) for the
 // runs kernel: lane i of a warp tests task 32 w + i, then the warp stores the
-// far tasks of its 32 one after the other, a task's 32 rows of 16 samples as
-// 128 16-byte pieces, 8 whole rows per store instruction (with a lane per
-// row, each store instruction half-filled 32 sectors: 2.9x slower).
+// far tasks of its 32 one after the other (runs_task_fill).
 __global__ void __launch_bounds__(256) synth_task_band_kernel(const up_synth_program P, const GridDev g, float band, float *__restrict__ out,
 	uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count) {
-	constexpr uint32_t R = RUN_R;
 	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
-	const uint32_t nruns = (nx + R - 1) / R, tny = (ny + 7) / 8, tnz = (nz + 3) / 4;
-	const uint32_t ntasks = nruns * tny * tnz; // < 2^31 (synth_grid_runs_kernel)
+	const uint32_t ntasks = ((nx + RUN_R - 1) / RUN_R) * ((ny + 7) / 8) * ((nz + 3) / 4); // < 2^31 (synth_grid_runs_kernel)
 	const uint32_t ngroups = (ntasks + 31) / 32;
 	const uint32_t lane = threadIdx.x & 31;
 	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ngroups; w += (gridDim.x * blockDim.x) >> 5) {
@@ -200,16 +196,11 @@ __global__ void __launch_bounds__(256) synth_task_band_kernel(const up_synth_pro
 		bool far = false;
 		float fv = 0.f;
 		if (t < ntasks) {
-			const uint32_t run = t % nruns, tile = t / nruns;
-			const uint32_t i0 = run * R, j0 = (tile % tny) * 8, k0 = (tile / tny) * 4;
-			const uint32_t i1 = min(i0 + R - 1, nx - 1), j1 = min(j0 + 7, ny - 1), k1 = min(k0 + 3, nz - 1);
-			const float x0 = grid_coord(g, 0, i0), x1 = grid_coord(g, 0, i1);
-			const float y0 = grid_coord(g, 1, j0), y1 = grid_coord(g, 1, j1);
-			const float z0 = grid_coord(g, 2, k0 + g.k0), z1 = grid_coord(g, 2, k1 + g.k0);
-			const V3f c = v3(0.5f * (x0 + x1), 0.5f * (y0 + y1), 0.5f * (z0 + z1));
-			const V3f h = v3(0.5f * fabsf(x1 - x0), 0.5f * fabsf(y1 - y0), 0.5f * fabsf(z1 - z0));
+			V3f c;
+			float hd;
+			runs_task_box(g, t, c, hd);
 			fv = synth_base<false>(P, c).v;
-			far = fabsf(fv) > (band + sqrtf(dot(h, h))) * 1.001f + 1e-5f; // false for NaN
+			far = fabsf(fv) > (band + hd) * 1.001f + 1e-5f; // false for NaN
 		}
 		const unsigned near = __ballot_sync(0xFFFFFFFFu, t < ntasks && !far);
 		uint32_t slot = 0;
@@ -220,22 +211,7 @@ __global__ void __launch_bounds__(256) synth_task_band_kernel(const up_synth_pro
 		for (unsigned fm = __ballot_sync(0xFFFFFFFFu, far); fm != 0u; fm &= fm - 1u) {
 			const int src = __ffs(fm) - 1;
 			const float v = __shfl_sync(0xFFFFFFFFu, fv, src);
-			const uint32_t tf = w * 32 + (uint32_t)src;
-			const uint32_t run = tf % nruns, tile = tf / nruns;
-			const uint32_t i0 = run * R, j0 = (tile % tny) * 8, k0 = (tile / tny) * 4;
-			#pragma unroll
-			for (uint32_t q = 0; q < 4; q++) {
-				const uint32_t piece = q * 32 + lane, rr = piece >> 2, x = i0 + (piece & 3) * 4;
-				const uint32_t jr = j0 + (rr & 7), kr = k0 + (rr >> 3);
-				if (jr >= ny || kr >= nz || x >= nx) continue;
-				float *o = out + ((uint64_t)kr * ny + jr) * nx + x;
-				if (x + 4 <= nx && ((uintptr_t)o & 15) == 0) {
-					*(float4 *)o = make_float4(v, v, v, v);
-				} else {
-					#pragma unroll 1
-					for (uint32_t r = 0; r < 4 && x + r < nx; r++) o[r] = v;
-				}
-			}
+			runs_task_fill(out, nx, ny, nz, w * 32 + (uint32_t)src, v);
 		}
 	}
 }
