@@ -89,6 +89,7 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 	extern __shared__ __align__(16) unsigned char runs_smem[];
 	A *acc = (A *)runs_smem + threadIdx.x;
 	constexpr int R = RUN_R;
+	constexpr int S = RUNS_T;
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t nz = g.n[2];
 	const uint32_t nrows = ny * nz;
@@ -118,33 +119,78 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 		if (lane == 0) t_next = atomicAdd(tasks, 1u); // taken ahead; read after the task
 		const uint32_t tt = task_list ? task_list[t] : t;
 		const uint32_t run = tt % nruns, tile = tt / nruns;
-		const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
-		const bool live = jr < ny && kr < nz;
+		const uint32_t j0 = (tile % tny) * 8, k0 = (tile / tny) * 4;
+		// this lane's row (rows past the grid evaluate its last row, unstored)
+		const uint32_t jr = j0 + (lane & 7), kr = k0 + (lane >> 3);
 		const uint32_t j = jr < ny ? jr : ny - 1, k = kr < nz ? kr : nz - 1;
-		const uint32_t row = k * ny + j;
 		rc.i0 = run * R;
 		rc.py = grid_coord(g, 1, j);
 		rc.pz = grid_coord(g, 2, k + g.k0);
-		synth_run<GRAD, T0, T1>(P, rc, R, acc, RUNS_T, band);
-		if (live) {
-			const uint64_t base = (uint64_t)row * nx + rc.i0;
+		synth_run<GRAD, T0, T1>(P, rc, R, acc, S, band);
+		if (GRAD) {
+			// value + gradient: the task's 32 rows, 8 per store instruction,
+			// lane l taking row 8 q + (l & 7) and samples 4 (l >> 3) .. + 3
+			// from another lane's accumulators (16-byte reads in phases of 8
+			// lanes, 8 consecutive slots); with a lane per row, each store
+			// instruction half-filled 32 sectors (1.3 % slower at 512^3).
 			// 16-byte stores only where every destination address is 16-byte
-			// aligned (caller pointers and plane offsets need not be)
+			// aligned (caller pointers and plane offsets need not be).
+			__syncwarp(); // every lane's accumulators are complete
+			const Acc4 *wacc = (const Acc4 *)runs_smem + (threadIdx.x & ~31u);
 			const bool full = rc.i0 + R <= nx;
-			const bool vec = full && ((uintptr_t)(out + base) & 15) == 0;
-			const bool vecg = GRAD && full &&
-				(((uintptr_t)(grad + base) | (uintptr_t)(grad + plane + base) | (uintptr_t)(grad + 2 * plane + base)) & 15) == 0;
+			const uint32_t x0 = 4 * (lane >> 3);
 			#pragma unroll 1
-			for (int r = 0; r < R; r += 4) {
+			for (uint32_t q = 0; q < 4; q++) {
+				const uint32_t rr = 8 * q + (lane & 7);
+				const uint32_t jj = j0 + (lane & 7), kk = k0 + q;
 				float v[4], gx[4], gy[4], gz[4];
 				#pragma unroll
-				for (int q = 0; q < 4; q++) {
-					if (GRAD) {
-						const Acc4 x = ((const Acc4 *)acc)[(r + q) * RUNS_T];
-						v[q] = x.v; gx[q] = x.gx; gy[q] = x.gy; gz[q] = x.gz;
+				for (int i = 0; i < 4; i++) {
+					const Acc4 x = wacc[(x0 + i) * S + rr];
+					v[i] = x.v; gx[i] = x.gx; gy[i] = x.gy; gz[i] = x.gz;
+				}
+				if (jj < ny && kk < nz && rc.i0 + x0 < nx) {
+					#pragma unroll
+					for (int i = 0; i < 4; i++) bad |= isnan(v[i]);
+					const uint64_t base = ((uint64_t)kk * ny + jj) * nx + rc.i0 + x0;
+					const bool vec = full && ((uintptr_t)(out + base) & 15) == 0;
+					const bool vecg = full &&
+						(((uintptr_t)(grad + base) | (uintptr_t)(grad + plane + base) | (uintptr_t)(grad + 2 * plane + base)) & 15) == 0;
+					if (vec) {
+						*(float4 *)(out + base) = make_float4(v[0], v[1], v[2], v[3]);
 					} else {
-						v[q] = ((const float *)acc)[(r + q) * RUNS_T];
+						#pragma unroll
+						for (int i = 0; i < 4; i++)
+							if (rc.i0 + x0 + i < nx) out[base + i] = v[i];
 					}
+					if (vecg) {
+						*(float4 *)(grad + base) = make_float4(gx[0], gx[1], gx[2], gx[3]);
+						*(float4 *)(grad + plane + base) = make_float4(gy[0], gy[1], gy[2], gy[3]);
+						*(float4 *)(grad + 2 * plane + base) = make_float4(gz[0], gz[1], gz[2], gz[3]);
+					} else {
+						#pragma unroll
+						for (int i = 0; i < 4; i++)
+							if (rc.i0 + x0 + i < nx) {
+								grad[base + i] = gx[i];
+								grad[plane + base + i] = gy[i];
+								grad[2 * plane + base + i] = gz[i];
+							}
+					}
+				}
+			}
+			__syncwarp(); // the reads are done before the next task writes
+		} else if (jr < ny && kr < nz) {
+			// values: each lane stores its own row (timed 1.3 % faster than
+			// the row-wise form above, whose 4-byte reads cost more)
+			const uint64_t base = ((uint64_t)kr * ny + jr) * nx + rc.i0;
+			const bool full = rc.i0 + R <= nx;
+			const bool vec = full && ((uintptr_t)(out + base) & 15) == 0;
+			#pragma unroll 1
+			for (int r = 0; r < R; r += 4) {
+				float v[4];
+				#pragma unroll
+				for (int q = 0; q < 4; q++) {
+					v[q] = ((const float *)acc)[(r + q) * S];
 					bad |= isnan(v[q]);
 				}
 				if (vec) {
@@ -153,21 +199,6 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 					#pragma unroll
 					for (int q = 0; q < 4; q++)
 						if (rc.i0 + r + q < nx) out[base + r + q] = v[q];
-				}
-				if (GRAD) {
-					if (vecg) {
-						*(float4 *)(grad + base + r) = make_float4(gx[0], gx[1], gx[2], gx[3]);
-						*(float4 *)(grad + plane + base + r) = make_float4(gy[0], gy[1], gy[2], gy[3]);
-						*(float4 *)(grad + 2 * plane + base + r) = make_float4(gz[0], gz[1], gz[2], gz[3]);
-					} else {
-						#pragma unroll
-						for (int q = 0; q < 4; q++)
-							if (rc.i0 + r + q < nx) {
-								grad[base + r + q] = gx[q];
-								grad[plane + base + r + q] = gy[q];
-								grad[2 * plane + base + r + q] = gz[q];
-							}
-					}
 				}
 			}
 		}
