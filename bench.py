@@ -50,8 +50,8 @@ METRIC = "SDF+grad Gsamples/s at 512^3 (fused value+gradient; plain and ms/plane
 UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
-# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (234.65 MB / 16,777,216)
-TRAFFIC_PER_SAMPLE_FUSED = 234.652160e6 / 16777216
+# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (244.77 MB / 16,777,216)
+TRAFFIC_PER_SAMPLE_FUSED = 244.771584e6 / 16777216
 
 
 def _pkg():
