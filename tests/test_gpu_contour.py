@@ -76,7 +76,9 @@ def _band_programs():
     progs = [("c1", W.sphere_fbm(), W.grid(W.GRID_C1, n=(96, 90, 84))),
              ("c2", W.torus_spheres_ridged_cellular(), W.grid(W.GRID_C2, n=(128, 120, 112))),
              # ragged work units: nx % 16, ny % 8 and nz % 4 nonzero, rows not 16-byte aligned
-             ("c2r", W.torus_spheres_ridged_cellular(), W.grid(W.GRID_C2, n=(131, 117, 103)))]
+             ("c2r", W.torus_spheres_ridged_cellular(), W.grid(W.GRID_C2, n=(131, 117, 103))),
+             # x extent a multiple of 16 (sign words written while sampling), samples ending mid-word
+             ("c2h", W.torus_spheres_ridged_cellular(), W.grid(W.GRID_C2, n=(112, 117, 103)))]
     for i in range(3):
         P = W.mixed_planet(rng)
         P.layer[0].amp[0] = 0.3  # a wide band
@@ -84,7 +86,7 @@ def _band_programs():
     return progs
 
 
-@pytest.mark.parametrize("k", range(6))
+@pytest.mark.parametrize("k", range(7))
 def test_narrow_band_contour_equals_full_grid(cuda, up, k):
     """up_contour samples its grid with the narrow band (noise skipped where
     |base| exceeds the noise bound plus one grid step); contouring the exactly

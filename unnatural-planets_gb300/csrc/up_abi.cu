@@ -218,6 +218,7 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 	c.g = make_grid(*grid);
 	const size_t np = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
 	const size_t nc = (size_t)(grid->n[0] - 1) * (grid->n[1] - 1) * (grid->n[2] - 1);
+	bool signs_ready = false; // the sampling launch wrote the sign words
 	if (values) {
 		c.d = (const float *)stage_in(ctx, B_GRID, values, np * 4);
 	} else {
@@ -225,7 +226,13 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 		reset_flag(ctx);
 		if (ctx->synthetic) {
 			uint32_t *tl = (uint32_t *)buf(ctx, B_TASKL, runs_task_count(c.g) * 4);
-			check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream, contour_band(ctx->prog, c.g), tl), "sdf grid kernel");
+			const float band = contour_band(ctx->prog, c.g);
+			uint32_t *sg = nullptr;
+			if (synth_grid_signs(ctx->prog, c.g, band)) {
+				sg = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(c.g) * 4);
+				signs_ready = true;
+			}
+			check(launch_synth_grid(ctx->prog, c.g, gd, nullptr, ctx->d_flag, ctx->stream, band, tl, sg), "sdf grid kernel");
 		} else {
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;
@@ -242,8 +249,8 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 	S.totals = (uint32_t *)buf(ctx, B_DC_TOT, 16);
 	S.cell_map = (uint32_t *)buf(ctx, B_DC_CMAP, nc * 4);
 	S.edge_map = (uint32_t *)buf(ctx, B_DC_EMAP, np * 12);
-	S.signs = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(c.g) * 4);
-	check(dc_count(c.d, c.g, S, ctx->stream), "contour count");
+	S.signs = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(c.g) * 4); // the same words when signs_ready
+	check(dc_count(c.d, c.g, S, ctx->stream, signs_ready), "contour count");
 	uint32_t tot[4] = {0, 0, 0, 0};
 	check(cudaMemcpyAsync(tot, S.totals, 12, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync totals");
 	check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");

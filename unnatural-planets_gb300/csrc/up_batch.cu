@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(128) batch_qef_kernel(const up_synth_program *
 	for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ncells; q += gridDim.x * blockDim.x) {
 		const uint32_t c = find_chunk(off, nchunks, q);
 		const BatchChunkDev &ch = chunks[c];
-		if (!dc_qef_item(BatchEvalF{planets + ch.planet}, d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
+		if (!dc_qef_item(BatchEvalF{planets + ch.planet}, NegFromValues{d + ch.pt_off}, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n,
 				pos + 3 * (uint64_t)q, nullptr))
 			fb_list[atomicAdd(fb_count, 1u)] = q;
 	}
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(32) batch_qef_fp64_kernel(const up_synth_progr
 		const uint32_t c = find_chunk(off, nchunks, q);
 		const BatchChunkDev &ch = chunks[c];
 		double vd[3];
-		dc_qef_vertex_fp64(d + ch.pt_off, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n, vd);
+		dc_qef_vertex_fp64(NegFromValues{d + ch.pt_off}, ch.g, cell_list[q], edge_map + 3 * (uint64_t)ch.pt_off, edge_t, edge_n, vd);
 		const float vc[3] = {(float)vd[0], (float)vd[1], (float)vd[2]};
 		dc_vertex_out(BatchEvalF{planets + ch.planet}, ch.g, cell_list[q], vc, pos + 3 * (uint64_t)q, nullptr);
 	}

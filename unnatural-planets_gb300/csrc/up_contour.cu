@@ -137,13 +137,15 @@ uint32_t dc_num_blocks(const GridDev &g) {
 }
 uint64_t dc_sign_words(const GridDev &g) { return ((uint64_t)g.n[0] * g.n[1] * g.n[2] + 31) / 32 + 2; }
 
-cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s) {
+cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s, bool signs_ready) {
 	const uint32_t npts = g.n[0] * g.n[1] * g.n[2];
 	const uint32_t nb = dc_num_blocks(g);
 	const uint64_t nalloc = dc_sign_words(g);
-	const uint64_t need = (nalloc + DC_SIGN_U * 8 - 1) / (DC_SIGN_U * 8); // 8 warps per block
-	const int pb = persistent_blocks((const void *)dc_signs_kernel, 256);
-	dc_signs_kernel<<<(unsigned)(need < (uint64_t)pb ? need : (uint64_t)pb), 256, 0, s>>>(d, npts, nalloc, S.signs);
+	if (!signs_ready) {
+		const uint64_t need = (nalloc + DC_SIGN_U * 8 - 1) / (DC_SIGN_U * 8); // 8 warps per block
+		const int pb = persistent_blocks((const void *)dc_signs_kernel, 256);
+		dc_signs_kernel<<<(unsigned)(need < (uint64_t)pb ? need : (uint64_t)pb), 256, 0, s>>>(d, npts, nalloc, S.signs);
+	}
 	dc_wcount_kernel<<<nb, DC_T, 0, s>>>(S.signs, nalloc, g, npts, nb, S.blk_counts);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;

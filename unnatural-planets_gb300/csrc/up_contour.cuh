@@ -214,8 +214,25 @@ __device__ __forceinline__ void dc_hermite_item(const E &ev, const float *__rest
 	n_out[2] = s.g.z * il;
 }
 
+// Sign sources (neg(q): sample q has d < 0) for the sign-change tests of the
+// QEF kernels, which look at all 12 edges of an active cell: the sampled
+// values, or the bit-packed sign words of contouring (dc_sign_words). A
+// narrow-band grid sampled with its sign words holds values only near the
+// surface (synth_task_band_kernel); its words are complete. The Hermite and
+// quad kernels read values only at the ends of sign-change edges, which lie
+// near the surface.
+struct NegFromValues {
+	const float *d;
+	__device__ __forceinline__ bool operator()(uint32_t q) const { return __ldg(d + q) < 0.f; }
+};
+struct NegFromBits {
+	const uint32_t *w;
+	__device__ __forceinline__ bool operator()(uint32_t q) const { return (__ldg(w + (q >> 5)) >> (q & 31)) & 1u; }
+};
+
 // FP64 QEF vertex (cell-local) of one active cell whose origin is grid point p
-static __device__ __noinline__ void dc_qef_vertex_fp64(const float *__restrict__ d, const GridDev &g, uint32_t p, const uint32_t *__restrict__ edge_map,
+template<class N>
+static __device__ __noinline__ void dc_qef_vertex_fp64(const N neg, const GridDev &g, uint32_t p, const uint32_t *__restrict__ edge_map,
 	const float *__restrict__ edge_t, const float *__restrict__ edge_n, double v[3]) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t sxy = nx * ny;
@@ -235,7 +252,7 @@ static __device__ __noinline__ void dc_qef_vertex_fp64(const float *__restrict__
 			else if (a == 1) { ii += u; kk += w; }
 			else { ii += u; jj += w; }
 			const uint32_t pe = (kk * ny + jj) * nx + ii;
-			if ((d[pe] < 0.f) == (d[pe + stride] < 0.f)) continue;
+			if (neg(pe) == neg(pe + stride)) continue;
 			const uint32_t eid = edge_map[3 * (uint64_t)pe + a];
 			const double t = (double)edge_t[eid];
 			double h[3] = {dc_coord(g, 0, ii), dc_coord(g, 1, jj), dc_coord(g, 2, kk)};
@@ -342,8 +359,8 @@ __device__ __forceinline__ void dc_vertex_out(const E &ev, const GridDev &g, uin
 // FP32 (no cancellation: the points are centred first). Returns false,
 // writing nothing, when the truncation decision is within FP32 rounding:
 // the cell then needs the FP64 solver (dc_qef_vertex_fp64, dc_vertex_out).
-template<class E>
-__device__ __forceinline__ bool dc_qef_item(const E &ev, const float *__restrict__ d, const GridDev &g, uint32_t p,
+template<class E, class N>
+__device__ __forceinline__ bool dc_qef_item(const E &ev, const N &neg, const GridDev &g, uint32_t p,
 	const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *vpos, float *vnrm) {
 	const uint32_t nx = g.n[0], ny = g.n[1];
 	const uint32_t sxy = nx * ny;
@@ -362,7 +379,7 @@ __device__ __forceinline__ bool dc_qef_item(const E &ev, const float *__restrict
 		const uint32_t pe = (kk * ny + jj) * nx + ii;
 		eid[sl] = 0;
 		P[sl][0] = P[sl][1] = P[sl][2] = 0.f;
-		if ((__ldg(d + pe) < 0.f) == (__ldg(d + pe + stride) < 0.f)) continue;
+		if (neg(pe) == neg(pe + stride)) continue;
 		eid[sl] = __ldg(edge_map + 3 * (uint64_t)pe + a);
 		const float t = __ldg(edge_t + eid[sl]);
 		P[sl][0] = a == 0 ? t : (float)u;
@@ -427,12 +444,12 @@ __global__ void __launch_bounds__(256) dc_hermite_kernel(const E ev, const float
 // into full warps there, the few FP64 cells do not hold whole warps of this
 // kernel on the slow FP64 pipe, and their latency overlaps dc_normal_kernel.
 template<class E>
-__global__ void __launch_bounds__(128) dc_qef_kernel(const E ev, const float *__restrict__ d, const GridDev g,
+__global__ void __launch_bounds__(128) dc_qef_kernel(const E ev, const uint32_t *__restrict__ signs, const GridDev g,
 	const uint32_t *__restrict__ cell_list, uint32_t ncells, const uint32_t *__restrict__ edge_map,
 	const float *__restrict__ edge_t, const float *__restrict__ edge_n, float *__restrict__ pos, uint8_t *__restrict__ fb_flag,
 	uint32_t *__restrict__ fb_list, uint32_t *__restrict__ fb_count) {
 	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
-		const bool ok = dc_qef_item(ev, d, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nullptr);
+		const bool ok = dc_qef_item(ev, NegFromBits{signs}, g, cell_list[c], edge_map, edge_t, edge_n, pos + 3 * (uint64_t)c, nullptr);
 		fb_flag[c] = ok ? 0 : 1;
 		if (!ok) fb_list[atomicAdd(fb_count, 1u)] = c;
 	}
@@ -457,7 +474,7 @@ __global__ void __launch_bounds__(256) dc_normal_kernel(const E ev, const float 
 // SM-wide resource on this part, so the few FP64 cells are spread over as
 // many SMs as there are cells (timed against 32 and 128 cells per block).
 template<class E>
-__global__ void __launch_bounds__(32) dc_qef_fp64_kernel(const E ev, const float *__restrict__ d, const GridDev g,
+__global__ void __launch_bounds__(32) dc_qef_fp64_kernel(const E ev, const uint32_t *__restrict__ signs, const GridDev g,
 	const uint32_t *__restrict__ cell_list, const uint32_t *__restrict__ edge_map, const float *__restrict__ edge_t,
 	const float *__restrict__ edge_n, float *__restrict__ pos, float *__restrict__ nrm, const uint32_t *__restrict__ fb_list,
 	const uint32_t *__restrict__ fb_count) {
@@ -466,7 +483,7 @@ __global__ void __launch_bounds__(32) dc_qef_fp64_kernel(const E ev, const float
 	for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
 		const uint32_t c = fb_list[e], p = cell_list[c];
 		double vd[3];
-		dc_qef_vertex_fp64(d, g, p, edge_map, edge_t, edge_n, vd);
+		dc_qef_vertex_fp64(NegFromBits{signs}, g, p, edge_map, edge_t, edge_n, vd);
 		const float vc[3] = {(float)vd[0], (float)vd[1], (float)vd[2]};
 		dc_vertex_out(ev, g, p, vc, pos + 3 * (uint64_t)c, nrm ? nrm + 3 * (uint64_t)c : nullptr);
 	}
@@ -491,7 +508,7 @@ cudaError_t dc_geometry_t(const E &ev, const float *d, const GridDev &g, DcScrat
 	if (e != cudaSuccess) return e;
 	const int b = persistent_blocks((const void *)dc_qef_kernel<E>, 128);
 	const uint32_t need = (ncells + 127) / 128;
-	dc_qef_kernel<E><<<need < (uint32_t)b ? need : (uint32_t)b, 128, 0, s>>>(ev, d, g, S.cell_list, ncells, S.edge_map, S.edge_t, S.edge_n, pos,
+	dc_qef_kernel<E><<<need < (uint32_t)b ? need : (uint32_t)b, 128, 0, s>>>(ev, S.signs, g, S.cell_list, ncells, S.edge_map, S.edge_t, S.edge_n, pos,
 		S.fb_flag, S.fb_list, fb_count);
 	// the FP64 cells (a grid as large as the count could need; blocks past it
 	// exit) on the side stream, beside the normals and quads on s
@@ -501,7 +518,7 @@ cudaError_t dc_geometry_t(const E &ev, const float *d, const GridDev &g, DcScrat
 		s64 = S.side;
 	}
 	const int b64 = persistent_blocks((const void *)dc_qef_fp64_kernel<E>, 32);
-	dc_qef_fp64_kernel<E><<<ncells < (uint32_t)b64 ? ncells : (uint32_t)b64, 32, 0, s64>>>(ev, d, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
+	dc_qef_fp64_kernel<E><<<ncells < (uint32_t)b64 ? ncells : (uint32_t)b64, 32, 0, s64>>>(ev, S.signs, g, S.cell_list, S.edge_map, S.edge_t, S.edge_n, pos,
 		nrm, S.fb_list, fb_count);
 	if (nrm) {
 		const int bn = persistent_blocks((const void *)dc_normal_kernel<E>, 256);

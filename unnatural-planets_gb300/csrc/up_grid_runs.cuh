@@ -457,6 +457,21 @@ __device__ __forceinline__ void runs_task_fill(float *__restrict__ out, uint32_t
 }
 #endif
 
+#ifdef __CUDACC__
+// Sign bits (bit p of the words: sample p < 0) of task t of an nx x ny x nz
+// grid whose x extent is a multiple of RUN_R: all of its samples have the
+// sign neg. Each of its 32 row segments is one aligned 16-bit half-word,
+// written by lane = row; warp-wide.
+__device__ __forceinline__ void runs_task_signs(uint16_t *__restrict__ signs, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t t, bool neg) {
+	static_assert(RUN_R == 16, "one 16-bit half-word per row segment");
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t nruns = nx / RUN_R, tny = (ny + 7) / 8;
+	const uint32_t run = t % nruns, tile = t / nruns;
+	const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
+	if (jr < ny && kr < nz) signs[(((uint64_t)kr * ny + jr) * nx + run * RUN_R) / 16] = neg ? 0xFFFFu : 0u;
+}
+#endif
+
 // one run: base shape plus layers into acc (R must be a multiple of CELL_SUB).
 // band > 0 (narrow band of contouring, values only): when every sample of the
 // warp's task has |base| > band, the layers are skipped and acc holds the

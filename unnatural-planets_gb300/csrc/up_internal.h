@@ -26,8 +26,13 @@ struct ModesDesc;
 // zeroed by the launcher, in stream order). task_list (runs_task_count
 // words, or null): lets a narrow-band value launch sample only the tasks
 // near the surface; the others get one value of the right sign per task.
+// signs (dc_sign_words, or null; only where synth_grid_signs holds and with
+// task_list): the launch writes the sign words of contouring, and values only
+// in the listed tasks (the others hold no sample that contouring reads by
+// value: NegFromBits in up_contour.cuh).
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s,
-	float band = 0.f, uint32_t *task_list = nullptr);
+	float band = 0.f, uint32_t *task_list = nullptr, uint32_t *signs = nullptr);
+bool synth_grid_signs(const up_synth_program &P, const GridDev &g, float band);
 // work units (tasks) of the x-coherent grid kernels on grid g
 uint64_t runs_task_count(const GridDev &g);
 // narrow band of contouring for program P on grid g (0 when unbounded)
@@ -68,7 +73,9 @@ size_t dc_scan_words(uint32_t nb);
 // exclusive scan of the three block-count arrays in place; totals[a] = sums
 cudaError_t dc_scan_blocks(uint32_t *blk, uint32_t nb, uint32_t *totals, cudaStream_t s);
 // pass 1: counts -> totals[0]=cells, [1]=edges, [2]=quads (device), returns after enqueue
-cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s);
+// signs_ready: S.signs already holds the sign words of d (written by the
+// sampling launch), so the sign pass is skipped
+cudaError_t dc_count(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s, bool signs_ready = false);
 // pass 2 (after the host knows the totals and sized the lists)
 cudaError_t dc_emit(const float *d, const GridDev &g, DcScratch &S, cudaStream_t s);
 cudaError_t dc_geometry_synth(const up_synth_program &P, const float *d, const GridDev &g, DcScratch &S, uint32_t ncells, uint32_t nedges,
