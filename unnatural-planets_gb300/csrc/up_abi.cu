@@ -237,8 +237,14 @@ int contour_count(up_context *ctx, int field, const up_grid *grid, const float *
 			float *o[3] = {nullptr, nullptr, nullptr};
 			o[field] = gd;
 			uint32_t *tl = (uint32_t *)buf(ctx, B_TASKL, runs_task_count(c.g) * 4);
-			check(launch_modes_grid(ctx->d_modes, ctx->modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream,
-				modes_contour_band(ctx->modes, field, c.g.step), tl), "sdf grid kernel");
+			const float band = modes_contour_band(ctx->modes, field, c.g.step);
+			uint32_t *sg = nullptr;
+			if (modes_grid_signs(ctx->modes, 1u << field, c.g, band)) {
+				sg = (uint32_t *)buf(ctx, B_DC_SIGNS, dc_sign_words(c.g) * 4);
+				signs_ready = true;
+			}
+			check(launch_modes_grid(ctx->d_modes, ctx->modes, 1u << field, c.g, o[0], o[1], o[2], nullptr, ctx->d_flag, ctx->stream, band, tl, sg),
+				"sdf grid kernel");
 		}
 		if (read_flag(ctx)) return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(field) + " sdf value");
 		c.d = gd;

@@ -458,17 +458,31 @@ __device__ __forceinline__ void runs_task_fill(float *__restrict__ out, uint32_t
 #endif
 
 #ifdef __CUDACC__
-// Sign bits (bit p of the words: sample p < 0) of task t of an nx x ny x nz
-// grid whose x extent is a multiple of RUN_R: all of its samples have the
-// sign neg. Each of its 32 row segments is one aligned 16-bit half-word,
-// written by lane = row; warp-wide.
-__device__ __forceinline__ void runs_task_signs(uint16_t *__restrict__ signs, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t t, bool neg) {
-	static_assert(RUN_R == 16, "one 16-bit half-word per row segment");
+// Sign bits of one row segment (bit p of the words: sample p < 0): samples
+// p0 .. p0 + 15 get the bits of m (bit r: sample p0 + r; bits past the row's
+// end clear). With the x extent a multiple of 16 (aligned) the segment is
+// an aligned half-word of its own, stored; otherwise its bits may share a
+// word with another task's and are OR-ed into words zeroed beforehand.
+__device__ __forceinline__ void runs_row_signs(uint32_t *__restrict__ signs, uint64_t p0, uint32_t m, bool aligned) {
+	if (aligned) {
+		((uint16_t *)signs)[p0 >> 4] = (uint16_t)m;
+		return;
+	}
+	if (!m) return;
+	const uint32_t sh = (uint32_t)(p0 & 31);
+	atomicOr(signs + (p0 >> 5), m << sh);
+	if (sh > 16) atomicOr(signs + (p0 >> 5) + 1, m >> (32 - sh));
+}
+// Sign bits of task t of an nx x ny x nz grid all of whose samples have the
+// sign neg; warp-wide, lane = row (runs_row_signs).
+__device__ __forceinline__ void runs_task_signs(uint32_t *__restrict__ signs, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t t, bool neg) {
 	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t nruns = nx / RUN_R, tny = (ny + 7) / 8;
+	const uint32_t nruns = (nx + RUN_R - 1) / RUN_R, tny = (ny + 7) / 8;
 	const uint32_t run = t % nruns, tile = t / nruns;
 	const uint32_t jr = (tile % tny) * 8 + (lane & 7), kr = (tile / tny) * 4 + (lane >> 3);
-	if (jr < ny && kr < nz) signs[(((uint64_t)kr * ny + jr) * nx + run * RUN_R) / 16] = neg ? 0xFFFFu : 0u;
+	const uint32_t i0 = run * RUN_R, len = nx - i0 < RUN_R ? nx - i0 : RUN_R;
+	if (jr < ny && kr < nz)
+		runs_row_signs(signs, ((uint64_t)kr * ny + jr) * nx + i0, neg ? (1u << len) - 1u : 0u, nx % RUN_R == 0);
 }
 #endif
 

@@ -33,14 +33,18 @@ struct ModesDesc;
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s,
 	float band = 0.f, uint32_t *task_list = nullptr, uint32_t *signs = nullptr);
 bool synth_grid_signs(const up_synth_program &P, const GridDev &g, float band);
+// zeroes the sign words before a launch writes them (runs_row_signs)
+cudaError_t runs_signs_clear(uint32_t *signs, const GridDev &g, cudaStream_t s);
 // work units (tasks) of the x-coherent grid kernels on grid g
 uint64_t runs_task_count(const GridDev &g);
 // narrow band of contouring for program P on grid g (0 when unbounded)
 float contour_band(const up_synth_program &P, const GridDev &g);
 cudaError_t launch_synth_points(const up_synth_program &P, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 // band > 0: narrow band of contouring one field (modes_contour_band)
+// task_list, signs: as launch_synth_grid (signs only where modes_grid_signs holds)
 cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &host, uint32_t fields_mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad, unsigned *flags,
-	cudaStream_t s, float band = 0.f, uint32_t *task_list = nullptr);
+	cudaStream_t s, float band = 0.f, uint32_t *task_list = nullptr, uint32_t *signs = nullptr);
+bool modes_grid_signs(const ModesDesc &host, uint32_t fields_mask, const GridDev &g, float band);
 cudaError_t launch_modes_points(const ModesDesc *M, int field, const float *xyz, uint64_t n, float *d, float *grad, unsigned *nanflag, cudaStream_t s);
 
 // adjoint: partial sums per block into partials (nblocks x ACC stride), then

@@ -74,7 +74,8 @@ constexpr int MRUN_SLOTS = 4; // slots 0-2: noise instances, then the three fiel
 // farther than the band from the shape's surface get shape(centre) in every
 // selected field; the others are listed for modes_grid_runs_kernel.
 __global__ void __launch_bounds__(256) modes_task_band_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g, float band,
-	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count) {
+	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count,
+	uint32_t *__restrict__ signs) {
 	const ModesDesc &M = *Mp;
 	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const uint32_t ntasks = ((nx + RUN_R - 1) / RUN_R) * ((ny + 7) / 8) * ((nz + 3) / 4); // < 2^31
@@ -101,6 +102,10 @@ __global__ void __launch_bounds__(256) modes_task_band_kernel(const ModesDesc *_
 		for (unsigned fm = __ballot_sync(0xFFFFFFFFu, far); fm != 0u; fm &= fm - 1u) {
 			const int src = __ffs(fm) - 1;
 			const float v = __shfl_sync(0xFFFFFFFFu, fv, src);
+			if (signs) { // one field; contouring reads no value of these samples
+				runs_task_signs(signs, nx, ny, nz, w * 32 + (uint32_t)src, v < 0.f);
+				continue;
+			}
 			#pragma unroll 1
 			for (int f = 0; f < 3; f++)
 				if (mask & (1u << f)) runs_task_fill(outs[f], nx, ny, nz, w * 32 + (uint32_t)src, v);
@@ -110,10 +115,12 @@ __global__ void __launch_bounds__(256) modes_task_band_kernel(const ModesDesc *_
 
 // task_list (narrow band only, or null): the tasks to sample, *list_count of
 // them, listed by modes_task_band_kernel, which has written the others.
+// signs (one field, with task_list; or null): the sign words of contouring
+// that field (synth_grid_runs_kernel).
 template<int EM>
 __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const ModesDesc *__restrict__ Mp, uint32_t mask, const GridDev g,
 	float *__restrict__ o0, float *__restrict__ o1, float *__restrict__ o2, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks,
-	float band, const uint32_t *__restrict__ task_list, const unsigned *__restrict__ list_count) {
+	float band, const uint32_t *__restrict__ task_list, const unsigned *__restrict__ list_count, uint32_t *__restrict__ signs) {
 	extern __shared__ __align__(16) float mruns_smem[];
 	constexpr int R = RUN_R;
 	float *tab = mruns_smem + threadIdx.x;
@@ -187,6 +194,12 @@ __global__ void __launch_bounds__(MRUNS_T, 3) modes_grid_runs_kernel(const Modes
 							if (rc.i0 + r + q < nx) o[base + r + q] = x[q];
 					}
 				}
+				if (signs) {
+					uint32_t neg = 0; // bit r: sample r < 0 (samples past the row clear)
+					#pragma unroll
+					for (int r = 0; r < R; r++) neg |= (src[r * MRUNS_T] < 0.f && rc.i0 + r < nx ? 1u : 0u) << r;
+					runs_row_signs(signs, base, neg, nx % R == 0);
+				}
 			}
 		}
 		t = __shfl_sync(0xFFFFFFFFu, t_next, 0);
@@ -242,8 +255,12 @@ static cudaError_t launch_mruns(K kernel, const GridDev &g, cudaStream_t s, unsi
 	return cudaGetLastError();
 }
 
+bool modes_grid_signs(const ModesDesc &H, uint32_t mask, const GridDev &g, float band) {
+	return band > 0.f && (mask == 1u || mask == 4u) && mrun_applies(H);
+}
 cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &H, uint32_t mask, const GridDev &g, float *o0, float *o1, float *o2, float *grad,
-	unsigned *flags, cudaStream_t s, float band, uint32_t *task_list) {
+	unsigned *flags, cudaStream_t s, float band, uint32_t *task_list, uint32_t *signs) {
+	if (signs && (grad || !task_list || !modes_grid_signs(H, mask, g, band))) return cudaErrorInvalidValue;
 	unsigned *const nanflag = flags, *const tasks = flags + 1, *const list_count = flags + 2;
 	const uint64_t n = (uint64_t)g.n[0] * g.n[1] * g.n[2];
 	if (n >= (1ull << 32)) return cudaErrorInvalidValue;
@@ -251,20 +268,25 @@ cudaError_t launch_modes_grid(const ModesDesc *M, const ModesDesc &H, uint32_t m
 	if ((mask & 5u) && mrun_applies(H)) {
 		const uint32_t *tl = nullptr;
 		const unsigned *tc = nullptr;
+		uint32_t *sg = nullptr;
 		if (band > 0.f && task_list) {
 			cudaError_t e = cudaMemsetAsync(list_count, 0, sizeof(unsigned), s);
 			if (e != cudaSuccess) return e;
+			if (signs) {
+				if ((e = runs_signs_clear(signs, g, s)) != cudaSuccess) return e;
+				sg = signs;
+			}
 			const uint64_t groups = (runs_task_count(g) + 31) / 32;
 			uint64_t blocks = (uint64_t)persistent_blocks((const void *)modes_task_band_kernel, 256);
 			if (blocks > (groups + 7) / 8) blocks = (groups + 7) / 8;
-			modes_task_band_kernel<<<(unsigned)blocks, 256, 0, s>>>(M, mask, g, band, o0, o1, o2, task_list, list_count);
+			modes_task_band_kernel<<<(unsigned)blocks, 256, 0, s>>>(M, mask, g, band, o0, o1, o2, task_list, list_count, sg);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			tl = task_list;
 			tc = list_count;
 		}
-		if (H.elevation == 2) return launch_mruns(modes_grid_runs_kernel<2>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc);
-		if (H.elevation == 3) return launch_mruns(modes_grid_runs_kernel<3>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc);
-		return launch_mruns(modes_grid_runs_kernel<4>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc);
+		if (H.elevation == 2) return launch_mruns(modes_grid_runs_kernel<2>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc, sg);
+		if (H.elevation == 3) return launch_mruns(modes_grid_runs_kernel<3>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc, sg);
+		return launch_mruns(modes_grid_runs_kernel<4>, g, s, tasks, M, mask, g, o0, o1, o2, nanflag, tasks, band, tl, tc, sg);
 	}
 	return launch_p(modes_grid_kernel<false>, n, s, M, mask, g, o0, o1, o2, grad, nanflag, band);
 }

@@ -81,12 +81,12 @@ static_assert(RUNS_T == 32 * RUNS_WARPS, "the x tables of up_grid_runs.cuh hold 
 // blocks (5 per SM, shared-memory bound: 5.25 ms at 512^3) and 2-warp blocks.
 // task_list (narrow band only, or null): the tasks to sample, *list_count of
 // them, listed by synth_task_band_kernel, which has written the others.
-// signs (value form with x extent a multiple of 16, or null): the bit-packed
-// d < 0 words of contouring (dc_sign_words), written 16 bits per row segment.
+// signs (value form with task_list, or null): the bit-packed d < 0 words of
+// contouring (dc_sign_words), written per row segment (runs_row_signs).
 template<bool GRAD, int T0, int T1>
 __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_synth_program P, const GridDev g, float *__restrict__ out,
 	float *__restrict__ grad, unsigned *__restrict__ nanflag, unsigned *__restrict__ tasks, float band,
-	const uint32_t *__restrict__ task_list, const unsigned *__restrict__ list_count, uint16_t *__restrict__ signs) {
+	const uint32_t *__restrict__ task_list, const unsigned *__restrict__ list_count, uint32_t *__restrict__ signs) {
 	typedef typename AccOf<GRAD>::T A;
 	extern __shared__ __align__(16) unsigned char runs_smem[];
 	A *acc = (A *)runs_smem + threadIdx.x;
@@ -203,11 +203,11 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 						if (rc.i0 + r + q < nx) out[base + r + q] = v[q];
 				}
 			}
-			if (signs) { // nx % 16 == 0: base % 16 == 0
-				uint32_t neg = 0; // bit r: sample r < 0
+			if (signs) {
+				uint32_t neg = 0; // bit r: sample r < 0 (samples past the row clear)
 				#pragma unroll
-				for (int r = 0; r < R; r++) neg |= (((const float *)acc)[r * S] < 0.f ? 1u : 0u) << r;
-				signs[base / 16] = (uint16_t)neg;
+				for (int r = 0; r < R; r++) neg |= (((const float *)acc)[r * S] < 0.f && rc.i0 + r < nx ? 1u : 0u) << r;
+				runs_row_signs(signs, base, neg, nx % R == 0);
 			}
 		}
 		t = __shfl_sync(0xFFFFFFFFu, t_next, 0);
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(RUNS_T, 3) synth_grid_runs_kernel(const up_syn
 // tests task 32 w + i, then the warp writes the far tasks of its 32 one after
 // the other (runs_task_signs, runs_task_fill).
 __global__ void __launch_bounds__(256) synth_task_band_kernel(const up_synth_program P, const GridDev g, float band, float *__restrict__ out,
-	uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count, uint16_t *__restrict__ signs) {
+	uint32_t *__restrict__ task_list, unsigned *__restrict__ list_count, uint32_t *__restrict__ signs) {
 	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const uint32_t ntasks = ((nx + RUN_R - 1) / RUN_R) * ((ny + 7) / 8) * ((nz + 3) / 4); // < 2^31 (synth_grid_runs_kernel)
 	const uint32_t ngroups = (ntasks + 31) / 32;
@@ -333,7 +333,15 @@ uint64_t runs_task_count(const GridDev &g) {
 	return (uint64_t)((g.n[0] + RUN_R - 1) / RUN_R) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4);
 }
 bool synth_grid_signs(const up_synth_program &P, const GridDev &g, float band) {
-	return band > 0.f && spec_of(P) == SPEC_PERLIN_CELL && g.n[0] % 16 == 0;
+	return band > 0.f && spec_of(P) == SPEC_PERLIN_CELL;
+}
+// Zeroes the sign words that runs_row_signs does not store: with the x extent
+// a multiple of 16, those past the last sample (and the upper half of the
+// last word when the samples end mid-word); otherwise all (bits are OR-ed).
+cudaError_t runs_signs_clear(uint32_t *signs, const GridDev &g, cudaStream_t s) {
+	const uint64_t npts = (uint64_t)g.n[0] * g.n[1] * g.n[2];
+	const uint64_t w0 = g.n[0] % RUN_R == 0 ? npts / 32 : 0;
+	return cudaMemsetAsync(signs + w0, 0, (dc_sign_words(g) - w0) * 4, s);
 }
 cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float *out, float *grad, unsigned *flags, cudaStream_t s, float band,
 	uint32_t *task_list, uint32_t *signs) {
@@ -344,26 +352,21 @@ cudaError_t launch_synth_grid(const up_synth_program &P, const GridDev &g, float
 	const Spec sp = spec_of(P);
 	if (sp == SPEC_PERLIN_CELL) {
 		if (grad) return launch_runs<true>(synth_grid_runs_kernel<true, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band,
-			(const uint32_t *)nullptr, (const unsigned *)nullptr, (uint16_t *)nullptr);
+			(const uint32_t *)nullptr, (const unsigned *)nullptr, (uint32_t *)nullptr);
 		if (band > 0.f && task_list) {
 			cudaError_t e = cudaMemsetAsync(list_count, 0, sizeof(unsigned), s);
 			if (e != cudaSuccess) return e;
-			if (signs) {
-				// the words past the last sample (and the upper half of the last
-				// word when the samples end mid-word) stay zero
-				const uint64_t npts = (uint64_t)g.n[0] * g.n[1] * g.n[2], w0 = npts / 32;
-				if ((e = cudaMemsetAsync(signs + w0, 0, (dc_sign_words(g) - w0) * 4, s)) != cudaSuccess) return e;
-			}
+			if (signs && (e = runs_signs_clear(signs, g, s)) != cudaSuccess) return e;
 			const uint64_t groups = (runs_task_count(g) + 31) / 32;
 			uint64_t blocks = (uint64_t)persistent_blocks((const void *)synth_task_band_kernel, 256);
 			if (blocks > (groups + 7) / 8) blocks = (groups + 7) / 8;
-			synth_task_band_kernel<<<(unsigned)blocks, 256, 0, s>>>(P, g, band, out, task_list, list_count, (uint16_t *)signs);
+			synth_task_band_kernel<<<(unsigned)blocks, 256, 0, s>>>(P, g, band, out, task_list, list_count, signs);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band,
-				(const uint32_t *)task_list, (const unsigned *)list_count, (uint16_t *)signs);
+				(const uint32_t *)task_list, (const unsigned *)list_count, signs);
 		}
 		return launch_runs<false>(synth_grid_runs_kernel<false, 2, CELL_EU_SUB>, g, s, tasks, P, g, out, grad, nanflag, tasks, band,
-			(const uint32_t *)nullptr, (const unsigned *)nullptr, (uint16_t *)nullptr);
+			(const uint32_t *)nullptr, (const unsigned *)nullptr, (uint32_t *)nullptr);
 	}
 	if (grad) {
 		if (sp == SPEC_PERLIN_CELL) return launch_persistent(synth_grid_kernel<true, 2, CELL_EU_SUB>, n, s, P, g, out, grad, nanflag, band);
