@@ -222,6 +222,15 @@ uint32_t hc_segment_base(const up_synth_program *P, float x0, float x1, float y,
 }
 
 // FastDiv (up_fastdiv.h): q[i] = n[i] / d by the multiply-shift
+// sign words of row segments (p0[i], bits m[i]) OR-ed as the unaligned
+// path of the grid kernels does (row_sign_parts)
+void hc_row_signs(const uint64_t *p0, const uint32_t *m, uint64_t count, uint32_t *words) {
+	for (uint64_t i = 0; i < count; i++) {
+		const up::RowSignParts q = up::row_sign_parts(p0[i], m[i]);
+		words[q.w] |= q.lo;
+		if (q.hi) words[q.w + 1] |= q.hi;
+	}
+}
 void hc_fastdiv(uint32_t d, const uint32_t *n, uint64_t count, uint32_t *q) {
 	const FastDiv f = FastDiv::of(d);
 	for (uint64_t i = 0; i < count; i++) q[i] = f.div(n[i]);

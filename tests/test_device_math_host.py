@@ -231,6 +231,36 @@ def test_fastdiv_exact(H):
         assert np.array_equal(q, n // np.uint32(d)), d
 
 
+def test_row_sign_bits_unaligned(H):
+    """Sign words written per 16-sample row segment (the narrow-band grid
+    kernels, x extents not a multiple of 16: bits OR-ed into zeroed words)
+    equal the words packed from the per-sample signs, for ragged rows whose
+    segments straddle word boundaries; the padding words stay zero."""
+    H.hc_row_signs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+    r = np.random.default_rng(21)
+    for nx in (17, 31, 33, 45, 100, 131, 200):
+        nrows = 37
+        npts = nx * nrows
+        neg = r.random(npts) < 0.5
+        neg[r.integers(0, npts, size=npts // 4)] = False
+        p0, m = [], []
+        for row in range(nrows):
+            for i0 in range(0, nx, 16):
+                ln = min(16, nx - i0)
+                bits = neg[row * nx + i0: row * nx + i0 + ln]
+                p0.append(row * nx + i0)
+                m.append(int(np.sum(bits.astype(np.uint64) << np.arange(ln, dtype=np.uint64))))
+        p0 = np.array(p0, dtype=np.uint64)
+        m = np.array(m, dtype=np.uint32)
+        nwords = (npts + 31) // 32 + 2
+        words = np.zeros(nwords, dtype=np.uint32)
+        H.hc_row_signs(p0.ctypes.data, m.ctypes.data, len(p0), words.ctypes.data)
+        padded = np.zeros(nwords * 32, dtype=bool)
+        padded[:npts] = neg
+        want = np.packbits(padded.reshape(-1, 8), axis=1, bitorder="little").reshape(-1).view("<u4")
+        assert np.array_equal(words, want), nx
+
+
 def test_narrow_band_runs_keep_signs(H, O):
     """The narrow-band runs of contouring (synth_run with a band, compiled for
     the host; there a run is one task): every sample keeps the sign of the

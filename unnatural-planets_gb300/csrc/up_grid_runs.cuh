@@ -457,6 +457,20 @@ __device__ __forceinline__ void runs_task_fill(float *__restrict__ out, uint32_t
 }
 #endif
 
+// The bits that a row segment's sign bits m (bit r: sample p0 + r; at most
+// 16 bits) occupy in the bit-packed words (bit p of word p / 32: sample p):
+// lo = m << (p0 % 32) in word w = p0 / 32, and hi = the bits past bit 31, in
+// word w + 1 (0 when none).
+struct RowSignParts { uint64_t w; uint32_t lo, hi; };
+UP_HD RowSignParts row_sign_parts(uint64_t p0, uint32_t m) {
+	const uint32_t sh = (uint32_t)(p0 & 31);
+	RowSignParts r;
+	r.w = p0 >> 5;
+	r.lo = m << sh;
+	r.hi = sh > 16 ? m >> (32 - sh) : 0u;
+	return r;
+}
+
 #ifdef __CUDACC__
 // Sign bits of one row segment (bit p of the words: sample p < 0): samples
 // p0 .. p0 + 15 get the bits of m (bit r: sample p0 + r; bits past the row's
@@ -469,9 +483,9 @@ __device__ __forceinline__ void runs_row_signs(uint32_t *__restrict__ signs, uin
 		return;
 	}
 	if (!m) return;
-	const uint32_t sh = (uint32_t)(p0 & 31);
-	atomicOr(signs + (p0 >> 5), m << sh);
-	if (sh > 16) atomicOr(signs + (p0 >> 5) + 1, m >> (32 - sh));
+	const RowSignParts q = row_sign_parts(p0, m);
+	atomicOr(signs + q.w, q.lo);
+	if (q.hi) atomicOr(signs + q.w + 1, q.hi);
 }
 // Sign bits of task t of an nx x ny x nz grid all of whose samples have the
 // sign neg; warp-wide, lane = row (runs_row_signs).
