@@ -222,6 +222,35 @@ uint32_t hc_segment_base(const up_synth_program *P, float x0, float x1, float y,
 }
 
 // FastDiv (up_fastdiv.h): q[i] = n[i] / d by the multiply-shift
+// grid of the host checks (the fields of GridDev that the task helpers read)
+struct HostGrid { uint32_t n[3]; float lo[3], step[3]; uint32_t k0; };
+
+// narrow band at the task level (synth_task_band_kernel): task_val[t] =
+// base(centre) for the tasks classified outside the band, NaN for the
+// listed ones; band as contour_band (noise bound + longest step, margins)
+float hc_task_band(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float *task_val) {
+	HostGrid g{{n[0], n[1], n[2]}, {lo[0], lo[1], lo[2]}, {step[0], step[1], step[2]}, 0u};
+	const float st = fmaxf(step[0], fmaxf(step[1], step[2]));
+	const float band = (synth_noise_bound(*P) + st) * 1.001f + 1e-5f;
+	const uint32_t ntasks = ((n[0] + RUN_R - 1) / RUN_R) * ((n[1] + 7) / 8) * ((n[2] + 3) / 4);
+	for (uint32_t t = 0; t < ntasks; t++) {
+		V3f c;
+		float hd;
+		runs_task_box(g, t, c, hd);
+		const float fv = synth_base<false>(*P, c).v;
+		task_val[t] = fabsf(fv) > (band + hd) * 1.001f + 1e-5f ? fv : NAN;
+	}
+	return band;
+}
+// base value at every grid sample (coordinates as the grid kernels form them)
+void hc_base_grid(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float *out) {
+	uint64_t q = 0;
+	for (uint32_t k = 0; k < n[2]; k++)
+		for (uint32_t j = 0; j < n[1]; j++)
+			for (uint32_t i = 0; i < n[0]; i++)
+				out[q++] = synth_base<false>(*P, v3(runs_coord(lo[0], step[0], i), runs_coord(lo[1], step[1], j), runs_coord(lo[2], step[2], k))).v;
+}
+
 // sign words of row segments (p0[i], bits m[i]) OR-ed as the unaligned
 // path of the grid kernels does (row_sign_parts)
 void hc_row_signs(const uint64_t *p0, const uint32_t *m, uint64_t count, uint32_t *words) {

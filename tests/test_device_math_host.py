@@ -261,6 +261,46 @@ def test_row_sign_bits_unaligned(H):
         assert np.array_equal(words, want), nx
 
 
+@pytest.mark.parametrize("k", range(4))
+def test_task_band_classification(H, O, k):
+    """The task-level narrow band (synth_task_band_kernel's test, compiled for
+    the host): every sample of a task classified outside the band has
+    |base| > band and the sign of the task's value, and so has the oracle's
+    exact SDF there (the layers stay below the band); most tasks of the
+    benchmark planet are outside. Ragged grids: x, y, z extents not multiples
+    of the task's 16 x 8 x 4."""
+    H.hc_task_band.restype = C.c_float
+    H.hc_task_band.argtypes = [C.POINTER(_abi().SynthProgram), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    H.hc_base_grid.argtypes = [C.POINTER(_abi().SynthProgram), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    W = workloads()
+    rng = np.random.default_rng(5)
+    cases = [(W.torus_spheres_ridged_cellular(), (131, 117, 103), 0.6), (W.torus_spheres_ridged_cellular(), (64, 56, 48), 0.0),
+             (W.mixed_planet(rng), (70, 41, 37), 0.3), (W.mixed_planet(rng), (96, 64, 60), 0.3)]
+    P, n, min_far = cases[k]
+    lo = np.full(3, -1.6, np.float32)
+    nn = np.array(n, np.uint32)
+    step = (np.float32(3.2) / (nn - 1).astype(np.float32)).astype(np.float32)
+    nt = (-(-n[0] // 16)) * (-(-n[1] // 8)) * (-(-n[2] // 4))
+    tv = np.empty(nt, np.float32)
+    band = H.hc_task_band(C.byref(P), lo.ctypes.data, step.ctypes.data, nn.ctypes.data, tv.ctypes.data)
+    base = np.empty(n[0] * n[1] * n[2], np.float32)
+    H.hc_base_grid(C.byref(P), lo.ctypes.data, step.ctypes.data, nn.ctypes.data, base.ctypes.data)
+    base = base.reshape(n[2], n[1], n[0])
+    kk, jj, ii = np.meshgrid(np.arange(n[2]), np.arange(n[1]), np.arange(n[0]), indexing="ij")
+    t = ii // 16 + (-(-n[0] // 16)) * (jj // 8 + (-(-n[1] // 8)) * (kk // 4))
+    far = ~np.isnan(tv)
+    assert far.mean() >= min_far
+    fs = far[t]
+    assert np.all(np.abs(base[fs]) > band)
+    assert np.all(np.sign(base[fs]) == np.sign(tv[t][fs]))
+    if k == 1:  # the exact SDF keeps the sign on a small grid
+        x = [lo[a] + np.arange(n[a], dtype=np.float32) * step[a] for a in range(3)]
+        zz, yy, xx = np.meshgrid(x[2], x[1], x[0], indexing="ij")
+        pts = np.stack([xx, yy, zz], -1).reshape(-1, 3)[fs.reshape(-1)]
+        d = O.synth_points(P, pts)
+        assert np.all(np.sign(d) == np.sign(tv[t][fs]))
+
+
 def test_narrow_band_runs_keep_signs(H, O):
     """The narrow-band runs of contouring (synth_run with a band, compiled for
     the host; there a run is one task): every sample keeps the sign of the

@@ -404,23 +404,31 @@ UP_HD void layer_run(const up_noise_layer &L, const RunCtx &rc, int R, typename 
 	}
 }
 
-#ifdef __CUDACC__
+// Grid coordinate lo + i step, rounded as the grid kernels form it
+UP_HD float runs_coord(float lo, float step, uint32_t i) {
+#ifdef __CUDA_ARCH__
+	return __fadd_rn(__fmul_rn((float)i, step), lo);
+#else
+	volatile float m = (float)i * step;
+	return m + lo;
+#endif
+}
 // Sample box of task t of the x-coherent grid kernels (below) on grid g
 // (fields n, lo, step, k0 of GridDev; coordinates as the kernels form them):
 // its centre c and half diagonal hd.
 template<class G>
-__device__ __forceinline__ void runs_task_box(const G &g, uint32_t t, V3f &c, float &hd) {
+UP_HD void runs_task_box(const G &g, uint32_t t, V3f &c, float &hd) {
 	const uint32_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const uint32_t nruns = (nx + RUN_R - 1) / RUN_R, tny = (ny + 7) / 8;
 	const uint32_t run = t % nruns, tile = t / nruns;
 	const uint32_t lo[3] = {run * RUN_R, (tile % tny) * 8, (tile / tny) * 4};
-	const uint32_t hi[3] = {min(lo[0] + RUN_R - 1, nx - 1), min(lo[1] + 7, ny - 1), min(lo[2] + 3, nz - 1)};
+	const uint32_t ext[3] = {RUN_R - 1, 7, 3}, last[3] = {nx - 1, ny - 1, nz - 1};
 	float cc[3], h2 = 0.f;
-	#pragma unroll
 	for (int a = 0; a < 3; a++) {
 		const uint32_t off = a == 2 ? g.k0 : 0u;
-		const float x0 = __fadd_rn(__fmul_rn((float)(lo[a] + off), g.step[a]), g.lo[a]);
-		const float x1 = __fadd_rn(__fmul_rn((float)(hi[a] + off), g.step[a]), g.lo[a]);
+		const uint32_t hi = lo[a] + ext[a] < last[a] ? lo[a] + ext[a] : last[a];
+		const float x0 = runs_coord(g.lo[a], g.step[a], lo[a] + off);
+		const float x1 = runs_coord(g.lo[a], g.step[a], hi + off);
 		const float h = 0.5f * fabsf(x1 - x0);
 		cc[a] = 0.5f * (x0 + x1);
 		h2 += h * h;
@@ -429,6 +437,7 @@ __device__ __forceinline__ void runs_task_box(const G &g, uint32_t t, V3f &c, fl
 	hd = sqrtf(h2);
 }
 
+#ifdef __CUDACC__
 // Task t of the x-coherent grid kernels (RUN_R samples along x of an 8 (y) x
 // 4 (z) tile of rows; tasks numbered x-run fastest) of an nx x ny x nz grid:
 // stores v at every sample, warp-wide (every lane calls it with the same t
