@@ -18,6 +18,9 @@ float modes_contour_band(const ModesDesc &D, int field, const float step[3]);
 
 using namespace up;
 
+// grid of the host checks (the fields of GridDev that the task helpers read)
+struct HostGrid { uint32_t n[3]; float lo[3], step[3]; uint32_t k0; };
+
 extern "C" {
 
 void hc_noise(int type, int dist, int op, uint32_t key, const float *xyz, uint64_t n, float *out, float *grad) {
@@ -222,9 +225,6 @@ uint32_t hc_segment_base(const up_synth_program *P, float x0, float x1, float y,
 }
 
 // FastDiv (up_fastdiv.h): q[i] = n[i] / d by the multiply-shift
-// grid of the host checks (the fields of GridDev that the task helpers read)
-struct HostGrid { uint32_t n[3]; float lo[3], step[3]; uint32_t k0; };
-
 // narrow band at the task level (synth_task_band_kernel): task_val[t] =
 // base(centre) for the tasks classified outside the band, NaN for the
 // listed ones; band as contour_band (noise bound + longest step, margins)
@@ -241,6 +241,21 @@ float hc_task_band(const up_synth_program *P, const float *lo, const float *step
 		task_val[t] = fabsf(fv) > (band + hd) * 1.001f + 1e-5f ? fv : NAN;
 	}
 	return band;
+}
+// reference-mode narrow band at the task level (modes_task_band_kernel):
+// task_val[t] = shape(centre) for the tasks classified outside the band,
+// NaN for the listed ones
+void hc_modes_task_band(void *d, const float *lo, const float *step, const uint32_t *n, float band, float *task_val) {
+	const ModesDesc &M = *(ModesDesc *)d;
+	HostGrid g{{n[0], n[1], n[2]}, {lo[0], lo[1], lo[2]}, {step[0], step[1], step[2]}, 0u};
+	const uint32_t ntasks = ((n[0] + RUN_R - 1) / RUN_R) * ((n[1] + 7) / 8) * ((n[2] + 3) / 4);
+	for (uint32_t t = 0; t < ntasks; t++) {
+		V3f c;
+		float hd;
+		runs_task_box(g, t, c, hd);
+		const float fv = shape_eval(M, vs(c.x, c.y, c.z));
+		task_val[t] = fabsf(fv) > (band + hd) * 1.001f + 1e-3f * (1.f + fabsf(fv)) ? fv : NAN;
+	}
 }
 // base value at every grid sample (coordinates as the grid kernels form them)
 void hc_base_grid(const up_synth_program *P, const float *lo, const float *step, const uint32_t *n, float *out) {

@@ -366,3 +366,40 @@ def test_modes_narrow_band_runs_keep_signs(H, O):
     assert (np.ptp(rows, axis=2) == 0).mean() > 0.3
     H.hc_modes_free(d)
 
+
+@pytest.mark.parametrize("shape,elevation,seed,n", [("sphere", "lakes", 4, (96, 50, 40)), ("torus", "islands", 2, (70, 41, 37)),
+                                                    ("box", "legacy", 3, (57, 64, 45))])
+def test_modes_task_band_classification(H, shape, elevation, seed, n):
+    """The reference-mode task-level band (modes_task_band_kernel's test,
+    compiled for the host): every sample of a task classified outside the
+    band has |shape| > band, and its land and navigation values have the
+    sign of the task's value; many tasks are outside. Ragged grids."""
+    H.hc_modes_create.restype = C.c_void_p
+    H.hc_modes_create.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_uint32]
+    H.hc_modes_free.argtypes = [C.c_void_p]
+    H.hc_modes_band.restype = C.c_float
+    H.hc_modes_band.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    H.hc_modes_grid_runs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    H.hc_modes_task_band.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+    d = H.hc_modes_create(shape.encode(), elevation.encode(), b"default", 0, 0, seed)
+    g = _abi().Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), n)
+    lo = np.array(g.lo[:], np.float32)
+    st = np.array([(g.hi[a] - g.lo[a]) / np.float32(g.n[a] - 1) for a in range(3)], np.float32)
+    nn = np.array(n, np.uint32)
+    full = [np.empty(g.count, np.float32) for _ in range(3)]
+    assert H.hc_modes_grid_runs(d, lo.ctypes.data, st.ctypes.data, nn.ctypes.data, 0.0, *[o.ctypes.data for o in full]) == 1
+    nt = (-(-n[0] // 16)) * (-(-n[1] // 8)) * (-(-n[2] // 4))
+    kk, jj, ii = np.meshgrid(np.arange(n[2]), np.arange(n[1]), np.arange(n[0]), indexing="ij")
+    t = (ii // 16 + (-(-n[0] // 16)) * (jj // 8 + (-(-n[1] // 8)) * (kk // 4))).reshape(-1)
+    for field in (0, 2):  # land, navigation
+        band = H.hc_modes_band(d, field, st.ctypes.data)
+        assert band > 0
+        tv = np.empty(nt, np.float32)
+        H.hc_modes_task_band(d, lo.ctypes.data, st.ctypes.data, nn.ctypes.data, band, tv.ctypes.data)
+        far = ~np.isnan(tv)
+        assert far.mean() > 0.2
+        fs = far[t]
+        assert np.all(np.abs(full[1][fs]) > band)  # water = the shape
+        assert np.all(np.sign(full[field][fs]) == np.sign(tv[t][fs]))
+    H.hc_modes_free(d)
+
