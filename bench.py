@@ -612,7 +612,7 @@ def run_only(args) -> None:
     print(json.dumps({"only": args.only, **r}), flush=True)
 
 
-def main():
+def make_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -622,7 +622,11 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads (atlas, adjoint, batch, fit, modes)")
     ap.add_argument("--only", choices=["atlas", "adjoint", "batch", "fit", "modes"],
                     help="run one secondary workload alone and print its result (profiling captures)")
-    args = ap.parse_args()
+    return ap
+
+
+def main():
+    args = make_parser().parse_args()
     if args.only:
         run_only(args)
     elif args.impl == "reference":
