@@ -75,19 +75,93 @@ def _cpu_model() -> str:
     return platform.processor() or platform.machine()
 
 
-def cpu_rate(P, grid, slabs: int, threads: int, grad: bool) -> tuple[float, float]:
-    """Samples/s of the oracle's FP32 callback path over `slabs` z-slabs from
-    the middle of the grid; returns (rate, seconds)."""
+def _slab_groups(nz: int, slabs: int, groups: int) -> list[tuple[int, int]]:
+    """`groups` runs of slabs // groups consecutive z-slabs, spread evenly over
+    the grid's z extent (each run keeps every host thread busy)"""
+    per = max(1, slabs // groups)
+    out = []
+    for k in range(groups):
+        z0 = min(nz - per, int((k + 0.5) * nz / groups) - per // 2)
+        out.append((max(0, z0), max(0, z0) + per))
+    return out
+
+
+def cpu_rate(P, grid, slabs: int, threads: int, grad: bool, groups: int = 4) -> tuple[float, float]:
+    """Samples/s of the oracle's FP32 callback path over `slabs` z-slabs in
+    `groups` runs spread evenly over z; returns (rate, seconds)."""
+    from oracle import oracle as O
+    runs = _slab_groups(int(grid.n[2]), slabs, groups)
+    t = time.perf_counter()
+    for z0, z1 in runs:
+        if grad:
+            O.synth_grid_fp32_cd(P, grid, z0, z1, CD_TAP, threads)
+        else:
+            O.synth_grid_fp32(P, grid, z0, z1, threads)
+    dt = time.perf_counter() - t
+    done = sum(z1 - z0 for z0, z1 in runs)
+    return int(grid.n[0]) * int(grid.n[1]) * done / dt, dt
+
+
+def cpu_planet(P, grid, threads: int) -> dict:
+    """The reference's CPU flow for one planet (meshGeneration.cpp:32-44,
+    updateByPosition then makeMesh): the oracle's FP32 per-sample callback
+    over the whole grid on `threads` host threads, then the oracle's dual
+    contouring of that grid (sequential, one thread)."""
     from oracle import oracle as O
     nz = int(grid.n[2])
-    z0 = nz // 2 - slabs // 2
-    t = time.perf_counter()
-    if grad:
-        O.synth_grid_fp32_cd(P, grid, z0, z0 + slabs, CD_TAP, threads)
-    else:
-        O.synth_grid_fp32(P, grid, z0, z0 + slabs, threads)
-    dt = time.perf_counter() - t
-    return int(grid.n[0]) * int(grid.n[1]) * slabs / dt, dt
+    t0 = time.perf_counter()
+    values = O.synth_grid_fp32(P, grid, 0, nz, threads)
+    t1 = time.perf_counter()
+    mesh = O.contour_synth(P, grid, values)
+    t2 = time.perf_counter()
+    return {"ms_per_planet": 1e3 * (t2 - t0), "sampling_ms": 1e3 * (t1 - t0), "contour_ms": 1e3 * (t2 - t1),
+            "vertices": int(len(mesh["positions"])), "triangles": int(len(mesh["indices"])) // 3,
+            "sample": f"the whole {grid.n[0]}x{grid.n[1]}x{nz} planet: FP32 per-sample callback on {threads} threads, "
+                      "then dual contouring on one thread (FP64 Hermite normals and QEF)"}
+
+
+def error_vs_fp64(up, W, planet, P, grid, d_dev, g_dev, mesh, threads: int) -> dict:
+    """Error of each result against the FP64 oracle (a checker run after the
+    timed regions): SDF values and gradients at 2^20 seeded grid points of the
+    512^3 grid, every vertex of the planet's mesh against the oracle's
+    contouring of the same FP32 grid, and every covered texel of the 4096^2
+    atlas of that mesh."""
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    n = grid.count
+    idx = np.unique(np.random.default_rng(2024).integers(0, n, size=1 << 20, dtype=np.int64))
+    it = torch.from_numpy(idx).cuda()
+    dv = d_dev[it].double().cpu().numpy()
+    gv = torch.stack([g_dev[it], g_dev[n + it], g_dev[2 * n + it]], dim=1).double().cpu().numpy()
+    ref, rg = O.synth_points(P, O.grid_positions_at(grid, idx), grad=True, threads=threads)
+    ev, eg = np.abs(dv - ref), np.abs(gv - rg).max(axis=1) / np.maximum(1.0, np.abs(rg).max(axis=1))
+    out = {"value": {"max": float(ev.max()), "rms": float(np.sqrt((ev ** 2).mean())), "samples": int(len(idx)), "tolerance": 1e-5},
+           "gradient": {"max_rel": float(eg.max()), "rms_rel": float(np.sqrt((eg ** 2).mean())),
+                        "frac_above_1e-4": float((eg > 1e-4).mean()), "samples": int(len(idx))}}
+    pos, nrm, tri = mesh
+    om = O.contour_synth(P, grid, d_dev.cpu().numpy())
+    step = np.array([(grid.hi[a] - grid.lo[a]) / (grid.n[a] - 1) for a in range(3)])
+    same = len(pos) == len(om["positions"]) and np.array_equal(tri, om["indices"])
+    if len(pos) == len(om["positions"]):
+        ec = (np.abs(pos.astype(np.float64) - om["positions"]) / step).max(axis=1)
+        out["vertices"] = {"max_cells": float(ec.max()), "rms_cells": float(np.sqrt((ec ** 2).mean())), "vertices": int(len(pos)),
+                           "frac_above_1e-3_cell": float((ec > 1e-3).mean())}
+    out["topology_bit_exact"] = bool(same)
+    wh = 4096
+    p2, n2, uv, i2 = W.quad_atlas(pos, nrm, tri, wh, wh)
+    got = planet.texture(1, p2, n2, uv, i2, wh, wh, dilation=7, floats=True)
+    want = O.texture(1, p2, n2, uv, i2, wh, wh, dilation=7, program=P, threads=threads)
+    cov = want["owner"] >= 0
+    tex = {"coverage_bit_exact": bool(np.array_equal(np.isnan(got["height_f"]), np.isnan(want["height_f"]))),
+           "covered_texels": int(cov.sum())}
+    for k in ("albedo", "special", "height"):
+        a, b = got[k + "_f"][cov].astype(np.float64), want[k + "_f"][cov].astype(np.float64)
+        e8 = np.abs(got[k].astype(int) - want[k].astype(int))[cov]
+        tex[k] = {"max": float(np.abs(a - b).max()), "rms": float(np.sqrt(((a - b) ** 2).mean())),
+                  "u8_frac_above_2": float((e8 > 2).mean())}
+    out["texels"] = tex
+    return out
 
 
 class Clocks:
@@ -394,16 +468,17 @@ def run_reference(args) -> None:
     P = W.torus_spheres_ridged_cellular()
     grid = W.grid(W.GRID_C2, n=(args.grid,) * 3)
     threads = os.cpu_count() or 1
-    slabs = min(max(2 * threads, 16), args.grid)
+    slabs = min(4 * threads, args.grid)
     for _ in range(args.warmup):
-        cpu_rate(P, grid, 2, threads, grad=True)
+        cpu_rate(P, grid, 4, threads, grad=True)
     rates, secs = [], []
     for _ in range(args.steps):
         r, s = cpu_rate(P, grid, slabs, threads, grad=True)
         rates.append(r)
         secs.append(s)
     value = args.steps * slabs * args.grid * args.grid / sum(secs) / 1e9
-    sample = f"{slabs} z-slabs of {args.grid}x{args.grid} ({slabs * args.grid * args.grid} samples) per step, value + 6-tap central-difference gradient (h={CD_TAP})"
+    sample = (f"{slabs} z-slabs of {args.grid}x{args.grid} ({slabs * args.grid * args.grid} samples) per step in 4 runs spread evenly over z, "
+              f"value + 6-tap central-difference gradient (h={CD_TAP})")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -534,11 +609,15 @@ def run_ours(args) -> None:
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     max_mhz = peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = sms * 128 * 2 * max_mhz * 1e6 / 1e12
-    # CPU baseline (rank 0, bounded sample)
+    # CPU baseline (rank 0, bounded samples): sampling rates over z-slabs
+    # spread over the grid, and one whole planet (sampling + contouring)
     threads = os.cpu_count() or 1
-    slabs = min(max(2 * threads, 16), args.grid)
+    slabs = min(4 * threads, args.grid)
     cpu_grad, cpu_s = cpu_rate(P, grid, slabs, threads, grad=True)
     cpu_plain, _ = cpu_rate(P, grid, slabs, threads, grad=False)
+    cpu_pl = _guard(lambda: cpu_planet(P, grid, threads))
+    # error of each result against the FP64 oracle (checker, after all timing)
+    errors = _guard(lambda: error_vs_fp64(up, W, planet, P, grid, d, g, (pos0, nrm0, idx0), threads))
     extras = {}
     if not args.no_extras:
         extras["atlas"] = _guard(lambda: extra_atlas(up, W, planet, stream, pos0, nrm0, idx0))
@@ -578,8 +657,12 @@ def run_ours(args) -> None:
                                   "peak_gbs": peaks.get("hbm_gbs"), "frac": (16 * N / (t_fused * 1e-3) / 1e9) / peaks["hbm_gbs"]
                                   if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}},
         "cpu_baseline": {"value": cpu_grad / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{slabs} z-slabs of {args.grid}x{args.grid} per leg; value+gradient by 6-tap central differences",
-                         "plain_value": cpu_plain / 1e9, "cpu": _cpu_model()},
+                         "sample": f"{slabs} z-slabs of {args.grid}x{args.grid} per leg in 4 runs spread evenly over z; "
+                                   "value+gradient by 6-tap central differences",
+                         "plain_value": cpu_plain / 1e9, "cpu": _cpu_model(),
+                         "ms_per_planet": cpu_pl.get("ms_per_planet") if isinstance(cpu_pl, dict) else None, "planet": cpu_pl},
+        "planet_speedup_vs_cpu": (cpu_pl["ms_per_planet"] / (sum(planet_ms) / len(planet_ms))) if "ms_per_planet" in cpu_pl else None,
+        "error_vs_fp64": errors,
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "extras": extras,

@@ -8,11 +8,13 @@
  *   - return an int status (UP_OK == 0, else a UP_ERR_* code; the message of
  *     the last failure on a context is available from up_last_error);
  *   - take caller-owned buffers as plain pointers plus explicit sizes; each
- *     pointer may be host memory or device memory of the context's GPU (the
- *     library inspects it with cudaPointerGetAttributes and copies host data
- *     through its own device scratch);
+ *     pointer may be host memory or device memory (the library inspects it
+ *     with cudaPointerGetAttributes: device memory of the context's GPU and
+ *     managed memory are used in place, host memory and memory of another
+ *     GPU are copied through the context's own device scratch);
  *   - are re-entrant across contexts; one context serves one host thread or
- *     one CUDA stream at a time.
+ *     one CUDA stream at a time (the per-point shims make a copy per thread);
+ *   - mark their span with an NVTX range named after the entry point.
  * Coordinates are FP32 in the reference's units. Grids are x-fastest:
  * index = (iz * ny + iy) * nx + ix.
  */
@@ -189,6 +191,14 @@ int up_context_set_theta(up_context *ctx, const float *theta, size_t n);
 size_t up_synth_theta_count(const up_synth_program *program);
 const char *up_status_string(int status);
 const char *up_last_error(const up_context *ctx);
+/* Bytes of device scratch the context holds now (staging and work buffers,
+ * grown on demand and kept for reuse; not the planet description). No
+ * reference counterpart. */
+size_t up_context_device_bytes(const up_context *ctx);
+/* Fault injection for tests, on the host only: the next count scratch
+ * allocations of any context fail as if the device were out of memory
+ * (the call returns UP_ERR_OOM). No reference counterpart. */
+void up_debug_fail_allocations(uint32_t count);
 /* Seed of noise instance slot i for planet seed s (math.cpp:73-77 replaced). */
 uint32_t up_instance_seed(uint32_t seed, uint32_t slot);
 
@@ -200,10 +210,19 @@ uint32_t up_instance_seed(uint32_t seed, uint32_t slot);
  * not NULL. Returns UP_ERR_NAN if any value is NaN. */
 int up_sdf_eval_points(up_context *ctx, int field, const float *xyz, size_t n, float *d, float *grad);
 
-/* Per-point shim with the reference callback's exact signature
- * (meshGeneration.cpp:12-15): evaluates the LAND field of the context made
- * current with up_set_current_context. Returns NaN on any error. One call is
- * one device round trip; batch callers use up_sdf_eval_points. */
+/* Per-point shims with the reference callback's exact signature
+ * (meshGeneration.cpp:12-15): up_sdf_land, up_sdf_water and
+ * up_sdf_navigation evaluate the LAND, WATER and NAVIGATION fields of the
+ * context installed with up_set_current_context. The reference calls its
+ * terrain functors from several threads at once (the navmesh, land and water
+ * pipelines and their chunk tasks, generator.cpp:159,215,432-439), so each
+ * calling thread evaluates on its own copy of the installed context (same
+ * planet; its own stream, flag and scratch), made on the thread's first call
+ * after the context was installed or its parameters changed
+ * (up_context_set_theta), and freed when the thread exits. Installing another
+ * context, or destroying the installed one, retires the copies. Returns NaN
+ * on any error. One call is one device round trip; batch callers use
+ * up_sdf_eval_points. */
 int up_set_current_context(up_context *ctx);
 float up_sdf_land(const float p[3]);
 float up_sdf_water(const float p[3]);
@@ -299,15 +318,15 @@ int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const 
  * the reference. It is for callers that cannot allocate device memory: an
  * engine that hands out all device memory from its own pool, or a process
  * that must not grow its device footprint after start-up. points, dL_dd and
- * dtheta must be device memory of the context's GPU (host buffers are
- * rejected with UP_ERR_INVALID_ARGUMENT: staging them would need an
- * allocation). The only scratch is a static device array of 2048 x 43 floats
- * (352 KiB) that every GPU that loads the library keeps until the process
- * exits; the kernel never launches more than 2048 blocks, so any point count
- * fits, and a parameter vector longer than 43 entries is rejected. The first
- * call on each device looks up the array's device address, so make that
- * first call before any stream capture begins. All calls share the array:
- * calls that overlap on the GPU race. */
+ * dtheta must be device memory of the context's GPU (host buffers and
+ * buffers of another GPU are rejected with UP_ERR_INVALID_ARGUMENT: staging
+ * them would need an allocation). The only scratch is a static device array
+ * of 2048 x 43 floats (352 KiB) that every GPU that loads the library keeps
+ * until the process exits; the kernel never launches more than 2048 blocks,
+ * so any point count fits, and a parameter vector longer than 43 entries is
+ * rejected. Creating the context looks up the array's device address (with
+ * the context's device current), so the call itself makes no runtime query.
+ * All calls share the array: calls that overlap on the GPU race. */
 int up_sdf_param_backward_noalloc(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta);
 
 /* ---------------------------------------------------------------- batching */

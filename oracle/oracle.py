@@ -50,6 +50,7 @@ def lib(fast: bool = False) -> C.CDLL:
         "orc_synth_grid_fp32": (None, [P, G, C.c_uint32, C.c_uint32, vp, C.c_int]),
         "orc_synth_grid_fp32_cd": (None, [P, G, C.c_uint32, C.c_uint32, C.c_float, vp, vp, C.c_int]),
         "orc_grid_positions": (None, [G, vp]),
+        "orc_grid_positions_at": (None, [G, vp, C.c_uint64, vp]),
         "orc_contour_synth": (vp, [P, G, vp]),
         "orc_mesh_counts": (None, [vp, vp]),
         "orc_mesh_copy": (None, [vp, vp, vp, vp, vp, vp]),
@@ -141,6 +142,14 @@ def synth_grid_fp32_cd(P, grid, z0, z1, h, threads, fast=True):
 def grid_positions(grid) -> np.ndarray:
     out = np.empty((grid.count, 3), np.float32)
     lib().orc_grid_positions(C.byref(grid), _p(out))
+    return out
+
+
+def grid_positions_at(grid, idx: np.ndarray) -> np.ndarray:
+    """positions of the samples with linear (x-fastest) indices idx"""
+    idx = np.ascontiguousarray(idx, np.uint64)
+    out = np.empty((idx.shape[0], 3), np.float32)
+    lib().orc_grid_positions_at(C.byref(grid), _p(idx), idx.shape[0], _p(out))
     return out
 
 

@@ -229,6 +229,19 @@ void orc_grid_positions(const up_grid *grid, float *out) {
 			}
 }
 
+// positions of the samples with linear indices idx[0..n) (x-fastest), the
+// same FP32 formula as orc_grid_positions
+void orc_grid_positions_at(const up_grid *grid, const uint64_t *idx, uint64_t n, float *out) {
+	const GridF g(*grid);
+	const uint64_t nx = g.n[0], ny = g.n[1];
+	for (uint64_t q = 0; q < n; q++) {
+		const uint64_t v = idx[q];
+		out[3 * q] = g.coord(0, (uint32_t)(v % nx));
+		out[3 * q + 1] = g.coord(1, (uint32_t)((v / nx) % ny));
+		out[3 * q + 2] = g.coord(2, (uint32_t)(v / (nx * ny)));
+	}
+}
+
 // ---------------------------------------------------------------- contour
 struct OrcMesh { ContourResult r; };
 

@@ -8,6 +8,7 @@
 #include "../../unnatural-planets_gb300/csrc/up_modes_runs.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_coloring.cuh"
 #include "../../unnatural-planets_gb300/csrc/up_fastdiv.h"
+#include "../../unnatural-planets_gb300/csrc/up_ptr.h"
 #include <string>
 
 namespace up {
@@ -65,6 +66,8 @@ int hc_synth_bwd(const up_synth_program *P, const float *xyz, uint64_t n, const 
 }
 
 uint32_t hc_lattice_hash(int x, int y, int z, uint32_t key) { return lattice_hash(x, y, z, key); }
+// where the C ABI takes a caller's buffer from (up_ptr.h): 0 host, 1 in place, 2 other GPU
+int hc_ptr_kind(int query_ok, int type, int device, int ctx_device) { return (int)ptr_kind(query_ok != 0, type, device, ctx_device); }
 uint32_t hc_corner_hash(int x, int y, int z, uint32_t key, int b) {
 	Cell c; c.ix = x; c.iy = y; c.iz = z; c.fx = c.fy = c.fz = 0.f;
 	return corner_hashes(c, key).h[b];

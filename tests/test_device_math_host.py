@@ -403,3 +403,21 @@ def test_modes_task_band_classification(H, shape, elevation, seed, n):
         assert np.all(np.sign(full[field][fs]) == np.sign(tv[t][fs]))
     H.hc_modes_free(d)
 
+
+
+def test_pointer_placement_rule(H):
+    """The C ABI uses a caller's buffer in place only when it is device memory
+    of the context's GPU or managed memory; host memory and memory of another
+    GPU are staged through the context's scratch (a kernel never makes a peer
+    access). Arguments: query ok, cudaMemoryType, attribute device, context device."""
+    H.hc_ptr_kind.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+    H.hc_ptr_kind.restype = C.c_int
+    HOST, LOCAL, OTHER = 0, 1, 2
+    assert H.hc_ptr_kind(1, 2, 0, 0) == LOCAL      # device memory of this GPU
+    assert H.hc_ptr_kind(1, 2, 3, 3) == LOCAL
+    assert H.hc_ptr_kind(1, 2, 1, 0) == OTHER      # device memory of another GPU
+    assert H.hc_ptr_kind(1, 2, 0, 1) == OTHER
+    assert H.hc_ptr_kind(1, 3, 5, 0) == LOCAL      # managed memory, any device
+    assert H.hc_ptr_kind(1, 1, 0, 0) == HOST       # page-locked host memory
+    assert H.hc_ptr_kind(1, 0, -2, 0) == HOST      # unregistered host memory
+    assert H.hc_ptr_kind(0, 2, 0, 0) == HOST       # the query failed: treated as host memory

@@ -41,6 +41,30 @@ def test_noalloc_adjoint_matches_allocating_entry_point(cuda, up):
         assert np.abs(got - ref).max() <= tol
 
 
+def test_noalloc_adjoint_allocates_nothing(cuda, up):
+    """A fresh context that only ever makes allocation-free calls holds no
+    device scratch afterwards (the context's scratch counter stays 0), and the
+    device's free memory does not move across a warmed-up call (the first
+    launch of a kernel may load its code)."""
+    torch = cuda
+    W = workloads()
+    planet = up.Planet(program=W.sphere_fbm())
+    x = torch.from_numpy(np.random.default_rng(5).uniform(-1.3, 1.3, size=(50000, 3)).astype(np.float32)).cuda()
+    w = torch.full((50000,), 1.0 / 50000, device="cuda")
+    out = torch.empty(len(W.theta_of(W.sphere_fbm())), device="cuda")
+
+    def call():
+        st = planet.lib.up_sdf_param_backward_noalloc(planet.h, x.data_ptr(), 50000, w.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        assert st == 0, planet.lib.up_last_error(planet.h)
+    call()   # warm-up: the first launch of a kernel may load its code
+    free0 = torch.cuda.mem_get_info()[0]
+    call()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert planet.lib.up_context_device_bytes(planet.h) == 0
+    assert np.all(np.isfinite(out.cpu().numpy()))
+
+
 def test_noalloc_adjoint_rejects_host_buffers(cuda, up):
     W = workloads()
     planet = up.Planet(program=W.sphere_fbm())

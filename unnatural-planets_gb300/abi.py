@@ -110,6 +110,8 @@ SIGNATURES = [
     ("up_synth_theta_count", C.c_size_t, [C.POINTER(SynthProgram)]),
     ("up_status_string", C.c_char_p, [C.c_int]),
     ("up_last_error", C.c_char_p, [C.c_void_p]),
+    ("up_context_device_bytes", C.c_size_t, [C.c_void_p]),
+    ("up_debug_fail_allocations", None, [C.c_uint32]),
     ("up_instance_seed", C.c_uint32, [C.c_uint32, C.c_uint32]),
     ("up_sdf_eval_points", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     ("up_set_current_context", C.c_int, [C.c_void_p]),

@@ -4,7 +4,10 @@
 #include "up_internal.h"
 #include "up_modes_desc.h"
 #include "up_noise.cuh"
+#include "up_ptr.h"
 #include "up_synth.cuh"
+
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cmath>
@@ -16,7 +19,9 @@
 #include <vector>
 
 namespace up {
-cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, cudaStream_t s);
+cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, float *scratch,
+	cudaStream_t s);
+cudaError_t noalloc_scratch_address(float **out);
 int build_modes(const up_modes &m, uint32_t seed, ModesDesc &D, std::string &shape_name, bool &double_sided, std::string &err);
 uint32_t instance_seed(uint32_t seed, uint32_t slot);
 float modes_contour_band(const ModesDesc &D, int field, const float step[3]);
@@ -48,6 +53,7 @@ enum BufSlot {
 struct up_context {
 	int device = 0;
 	cudaStream_t stream = nullptr;
+	bool owns_stream = false; // per-thread copies of the shims create their own stream
 	bool synthetic = false;
 	up_synth_program prog{};
 	ModesDesc modes{};
@@ -56,6 +62,7 @@ struct up_context {
 	bool double_sided = false;
 	std::string last_error;
 	unsigned *d_flag = nullptr;
+	float *noalloc_scratch = nullptr; // device address of the static scratch of up_sdf_param_backward_noalloc
 	struct Buf { void *p = nullptr; size_t n = 0; } bufs[B_COUNT];
 	void *batch = nullptr; // planned batch (up_batch.cu)
 	// device-to-host pipeline of up_sdf_grid: copies of slab k overlap the
@@ -67,7 +74,23 @@ struct up_context {
 
 namespace {
 
-std::atomic<up_context *> g_current{nullptr};
+// The context installed for the per-point shims (up_set_current_context),
+// and a generation number that changes whenever the installed context
+// changes or is destroyed: a thread's copy of an older generation is stale.
+std::mutex g_current_mu;
+up_context *g_current = nullptr;
+uint64_t g_current_gen = 0;
+
+// Host-side fault injection: the next g_fail_allocs scratch allocations fail
+// as if cudaMalloc had returned cudaErrorMemoryAllocation (no GPU involved).
+std::atomic<uint32_t> g_fail_allocs{0};
+
+// NVTX range around one entry point (shows in Nsight timelines; free when no
+// tool is attached)
+struct NvtxRange {
+	explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+	~NvtxRange() { nvtxRangePop(); }
+};
 
 struct Fail {
 	int code;
@@ -106,37 +129,42 @@ void *buf(up_context *ctx, int slot, size_t bytes) {
 	b.p = nullptr;
 	b.n = 0;
 	size_t want = bytes + bytes / 8;
+	uint32_t f = g_fail_allocs.load();
+	while (f > 0 && !g_fail_allocs.compare_exchange_weak(f, f - 1)) {}
+	if (f > 0) throw Fail{UP_ERR_OOM, "cudaMalloc: out of memory (injected)"};
 	check(cudaMalloc(&b.p, want), "cudaMalloc");
 	b.n = want;
 	return b.p;
 }
 
-bool is_device(const void *p) {
+// true when the kernels of ctx may read or write p in place: device memory
+// of the context's own GPU, or managed memory. Host memory and memory of
+// another GPU are copied through the context's scratch (cudaMemcpyDefault
+// resolves either through unified addressing).
+bool is_local(const up_context *ctx, const void *p) {
 	if (!p) return false;
 	cudaPointerAttributes a;
-	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-		cudaGetLastError();
-		return false;
-	}
-	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+	const bool ok = cudaPointerGetAttributes(&a, p) == cudaSuccess;
+	if (!ok) cudaGetLastError();
+	return ptr_kind(ok, ok ? (int)a.type : 0, ok ? a.device : -1, ctx->device) == PTR_LOCAL;
 }
 
 // device view of a caller input: the pointer itself, or a staged copy
 const void *stage_in(up_context *ctx, int slot, const void *p, size_t bytes) {
-	if (is_device(p)) return p;
+	if (is_local(ctx, p)) return p;
 	void *d = buf(ctx, slot, bytes);
-	check(cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync H2D");
+	check(cudaMemcpyAsync(d, p, bytes, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync stage in");
 	return d;
 }
 // device target for a caller output: the pointer itself, or scratch
 void *stage_out(up_context *ctx, int slot, void *p, size_t bytes) {
 	if (!p) return nullptr;
-	if (is_device(p)) return p;
+	if (is_local(ctx, p)) return p;
 	return buf(ctx, slot, bytes);
 }
-void finish_out(up_context *ctx, void *host, const void *dev, size_t bytes) {
-	if (!host || host == dev) return;
-	check(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync D2H");
+void finish_out(up_context *ctx, void *dst, const void *dev, size_t bytes) {
+	if (!dst || dst == dev) return;
+	check(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync stage out");
 }
 
 void set_device(up_context *ctx) { check(cudaSetDevice(ctx->device), "cudaSetDevice"); }
@@ -167,11 +195,18 @@ int init_context(up_context *ctx) {
 	}
 	check(cudaGetDevice(&ctx->device), "cudaGetDevice");
 	check(cudaMalloc(&ctx->d_flag, 16), "cudaMalloc flag");
+	// the static scratch of up_sdf_param_backward_noalloc: its module is loaded
+	// and its device address looked up now, at set-up, with the context's
+	// device current, so the allocation-free entry point neither grows the
+	// device footprint nor queries the runtime later (for example inside a
+	// stream capture)
+	check(noalloc_scratch_address(&ctx->noalloc_scratch), "cudaGetSymbolAddress (allocation-free scratch)");
 	return UP_OK;
 }
 
 template<class F>
-int guarded(up_context *ctx, F &&f) {
+int guarded(up_context *ctx, const char *name, F &&f) {
+	NvtxRange range(name);
 	try {
 		return f();
 	} catch (const Fail &e) {
@@ -328,9 +363,9 @@ int sdf_grid_pipelined(up_context *ctx, uint32_t mask, const GridDev &g, float *
 		const size_t off = plane * z0;
 		for (int f = 0; f < 3; f++)
 			if (mask >> f & 1u)
-				check(cudaMemcpyAsync(out[f] + off, o[f], cn * 4, cudaMemcpyDeviceToHost, ctx->copy_stream), "cudaMemcpyAsync D2H");
+				check(cudaMemcpyAsync(out[f] + off, o[f], cn * 4, cudaMemcpyDefault, ctx->copy_stream), "cudaMemcpyAsync D2H");
 		for (int a = 0; grad && a < 3; a++)
-			check(cudaMemcpyAsync(grad + (size_t)a * n + off, dg + (size_t)a * cn, cn * 4, cudaMemcpyDeviceToHost, ctx->copy_stream),
+			check(cudaMemcpyAsync(grad + (size_t)a * n + off, dg + (size_t)a * cn, cn * 4, cudaMemcpyDefault, ctx->copy_stream),
 				"cudaMemcpyAsync D2H");
 		check(cudaEventRecord(ctx->ev_copied[b], ctx->copy_stream), "cudaEventRecord");
 	}
@@ -342,6 +377,28 @@ int sdf_grid_pipelined(up_context *ctx, uint32_t mask, const GridDev &g, float *
 		return fail(ctx, UP_ERR_NAN, std::string("invalid ") + field_word(f) + " sdf value");
 	}
 	return (int)UP_OK;
+}
+
+// frees everything a context holds (no lock: callers deal with the installed context)
+void destroy_context(up_context *ctx) {
+	cudaSetDevice(ctx->device);
+	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+	for (auto &b : ctx->bufs) if (b.p) cudaFree(b.p);
+	if (ctx->d_flag) cudaFree(ctx->d_flag);
+	if (ctx->d_modes) cudaFree(ctx->d_modes);
+	if (ctx->batch) batch_state_free(ctx->batch);
+	if (ctx->copy_stream) {
+		cudaStreamSynchronize(ctx->copy_stream);
+		cudaStreamDestroy(ctx->copy_stream);
+	}
+	for (int b = 0; b < 2; b++) {
+		if (ctx->ev_done[b]) cudaEventDestroy(ctx->ev_done[b]);
+		if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
+	}
+	if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+	if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+	if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+	delete ctx;
 }
 
 } // namespace
@@ -392,7 +449,7 @@ int up_context_create(const up_modes *modes, const up_seeds *seeds, up_context *
 		delete ctx;
 		return st;
 	}
-	const int r = guarded(ctx, [&]() {
+	const int r = guarded(ctx, "up_context_create", [&]() {
 		const int st2 = init_context(ctx);
 		if (st2 != UP_OK) return st2;
 		check(cudaMalloc(&ctx->d_modes, sizeof(ModesDesc)), "cudaMalloc planet description");
@@ -418,7 +475,7 @@ int up_context_create_synthetic(const up_synth_program *program, up_context **ou
 	ctx->synthetic = true;
 	ctx->prog = *program;
 	ctx->shape_name = "synthetic";
-	const int r = guarded(ctx, [&]() { return init_context(ctx); });
+	const int r = guarded(ctx, "up_context_create_synthetic", [&]() { return init_context(ctx); });
 	if (r != UP_OK) {
 		delete ctx;
 		return r;
@@ -429,27 +486,25 @@ int up_context_create_synthetic(const up_synth_program *program, up_context **ou
 
 int up_context_destroy(up_context *ctx) {
 	if (!ctx) return UP_ERR_INVALID_ARGUMENT;
-	up_context *expect = ctx;
-	g_current.compare_exchange_strong(expect, nullptr);
-	cudaSetDevice(ctx->device);
-	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-	for (auto &b : ctx->bufs) if (b.p) cudaFree(b.p);
-	if (ctx->d_flag) cudaFree(ctx->d_flag);
-	if (ctx->d_modes) cudaFree(ctx->d_modes);
-	if (ctx->batch) batch_state_free(ctx->batch);
-	if (ctx->copy_stream) {
-		cudaStreamSynchronize(ctx->copy_stream);
-		cudaStreamDestroy(ctx->copy_stream);
+	{
+		std::lock_guard<std::mutex> lock(g_current_mu);
+		if (g_current == ctx) {
+			g_current = nullptr;
+			g_current_gen++;
+		}
 	}
-	for (int b = 0; b < 2; b++) {
-		if (ctx->ev_done[b]) cudaEventDestroy(ctx->ev_done[b]);
-		if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
-	}
-	if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-	if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
-	delete ctx;
+	destroy_context(ctx);
 	return UP_OK;
 }
+
+size_t up_context_device_bytes(const up_context *ctx) {
+	if (!ctx) return 0;
+	size_t n = 0;
+	for (const auto &b : ctx->bufs) n += b.n;
+	return n;
+}
+
+void up_debug_fail_allocations(uint32_t count) { g_fail_allocs.store(count); }
 
 int up_context_set_stream(up_context *ctx, void *stream) {
 	if (!ctx) return UP_ERR_INVALID_ARGUMENT;
@@ -482,11 +537,15 @@ int up_context_set_theta(up_context *ctx, const float *theta, size_t n) {
 			for (int s = 0; s < p.n_spheres; s++) p.sphere[s][3] = theta[t++];
 			p.k = theta[t++];
 	}
+	std::lock_guard<std::mutex> lock(g_current_mu);
+	if (g_current == ctx) g_current_gen++; // the shims' per-thread copies are stale
 	return UP_OK;
 }
 
 int up_set_current_context(up_context *ctx) {
-	g_current.store(ctx);
+	std::lock_guard<std::mutex> lock(g_current_mu);
+	g_current = ctx;
+	g_current_gen++;
 	return UP_OK;
 }
 
@@ -494,7 +553,7 @@ int up_sdf_eval_points(up_context *ctx, int field, const float *xyz, size_t n, f
 	if (!ctx || !xyz || !d || n == 0) return UP_ERR_INVALID_ARGUMENT;
 	if (field < 0 || field > 4) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "bad field");
 	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_sdf_eval_points", [&]() {
 		set_device(ctx);
 		const float *dx = (const float *)stage_in(ctx, B_IN0, xyz, n * 12);
 		float *dd = (float *)stage_out(ctx, B_OUT0, d, n * 4);
@@ -509,13 +568,78 @@ int up_sdf_eval_points(up_context *ctx, int field, const float *xyz, size_t n, f
 	});
 }
 
-static float shim(int field, const float p[3]) {
-	up_context *ctx = g_current.load();
-	if (!ctx || !p) return NAN;
+} // extern "C"
+
+namespace {
+
+// A copy of src for one host thread: the same planet description, its own
+// stream, flag and scratch. Device memory of the copy is separate from src,
+// so copies never share staging buffers, NaN flags or error messages.
+up_context *clone_for_thread(const up_context *src) {
+	up_context *c = new (std::nothrow) up_context();
+	if (!c) return nullptr;
+	c->synthetic = src->synthetic;
+	c->prog = src->prog;
+	c->modes = src->modes;
+	c->shape_name = src->shape_name;
+	c->double_sided = src->double_sided;
+	const int r = guarded(c, "up_sdf_shim_context", [&]() {
+		check(cudaSetDevice(src->device), "cudaSetDevice");
+		const int st = init_context(c);
+		if (st != UP_OK) return st;
+		check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+		c->owns_stream = true;
+		if (!c->synthetic) {
+			check(cudaMalloc(&c->d_modes, sizeof(ModesDesc)), "cudaMalloc planet description");
+			check(cudaMemcpy(c->d_modes, &c->modes, sizeof(ModesDesc), cudaMemcpyHostToDevice), "cudaMemcpy planet description");
+		}
+		return (int)UP_OK;
+	});
+	if (r != UP_OK) {
+		destroy_context(c);
+		return nullptr;
+	}
+	return c;
+}
+
+// The calling thread's copy of the installed context, made on the thread's
+// first shim call after up_set_current_context (or up_context_set_theta of
+// the installed context) and destroyed when the thread exits.
+struct ShimCopy {
+	uint64_t gen = 0;
+	up_context *ctx = nullptr;
+	~ShimCopy() {
+		if (ctx) destroy_context(ctx);
+	}
+};
+thread_local ShimCopy t_shim;
+
+up_context *shim_context() {
+	std::lock_guard<std::mutex> lock(g_current_mu); // the installed context stays alive while it is copied
+	if (!g_current) return nullptr;
+	if (t_shim.ctx && t_shim.gen == g_current_gen) return t_shim.ctx;
+	if (t_shim.ctx) {
+		destroy_context(t_shim.ctx);
+		t_shim.ctx = nullptr;
+	}
+	t_shim.ctx = clone_for_thread(g_current);
+	t_shim.gen = g_current_gen;
+	return t_shim.ctx;
+}
+
+float shim(int field, const float p[3]) {
+	if (!p) return NAN;
+	up_context *ctx = shim_context();
+	if (!ctx) return NAN;
 	float d = NAN;
 	if (up_sdf_eval_points(ctx, field, p, 1, &d, nullptr) != UP_OK) return NAN;
 	return d;
 }
+
+} // namespace
+
+extern "C" {
+
 float up_sdf_land(const float p[3]) { return shim(UP_FIELD_LAND, p); }
 float up_sdf_water(const float p[3]) { return shim(UP_FIELD_WATER, p); }
 float up_sdf_navigation(const float p[3]) { return shim(UP_FIELD_NAVIGATION, p); }
@@ -527,14 +651,14 @@ int up_sdf_grid(up_context *ctx, uint32_t mask, const up_grid *grid, float *cons
 	if (ctx->synthetic && mask != 1u) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
 	for (int f = 0; f < 3; f++)
 		if ((mask >> f & 1u) && !out[f]) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "missing output for a selected field");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_sdf_grid", [&]() {
 		set_device(ctx);
 		const GridDev g = make_grid(*grid);
 		const size_t n = (size_t)grid->n[0] * grid->n[1] * grid->n[2];
-		// every output in host memory and a grid large enough: pipelined slabs
-		bool host_only = n >= GRID_PIPE_MIN && !(grad && is_device(grad));
+		// no output on the context's GPU and a grid large enough: pipelined slabs
+		bool host_only = n >= GRID_PIPE_MIN && !(grad && is_local(ctx, grad));
 		for (int f = 0; f < 3; f++)
-			if ((mask >> f & 1u) && is_device(out[f])) host_only = false;
+			if ((mask >> f & 1u) && is_local(ctx, out[f])) host_only = false;
 		if (host_only) return sdf_grid_pipelined(ctx, mask, g, out, grad);
 		float *o[3] = {nullptr, nullptr, nullptr};
 		for (int f = 0; f < 3; f++)
@@ -559,7 +683,7 @@ int up_contour(up_context *ctx, int field, const up_grid *grid, const float *val
 	if (!ctx || !valid_grid(grid) || !mesh) return UP_ERR_INVALID_ARGUMENT;
 	if (field < 0 || field > 2) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "contour field must be LAND, WATER or NAVIGATION");
 	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_contour", [&]() {
 		set_device(ctx);
 		ContourRun c;
 		const int st = contour_count(ctx, field, grid, values, c);
@@ -584,7 +708,7 @@ int up_mesh_generate_base(up_context *ctx, int field, const up_grid *grid, const
 	if (!ctx || !valid_grid(grid) || !mesh) return UP_ERR_INVALID_ARGUMENT;
 	if (field < 0 || field > 2) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "base mesh field must be LAND, WATER or NAVIGATION");
 	if (ctx->synthetic && field != UP_FIELD_LAND) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "synthetic programs have only the LAND field");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_mesh_generate_base", [&]() {
 		set_device(ctx);
 		ContourRun c;
 		const int st = contour_count(ctx, field, grid, values, c);
@@ -644,7 +768,7 @@ int up_mesh_generate_base(up_context *ctx, int field, const up_grid *grid, const
 
 int up_image_special_to_gltf_pbr(up_context *ctx, const uint8_t *special, uint32_t width, uint32_t height, uint8_t *pbr) {
 	if (!ctx || !special || !pbr || width == 0 || height == 0) return UP_ERR_INVALID_ARGUMENT;
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_image_special_to_gltf_pbr", [&]() {
 		set_device(ctx);
 		const size_t n = (size_t)width * height;
 		const uint8_t *si = (const uint8_t *)stage_in(ctx, B_IN0, special, n * 2);
@@ -658,7 +782,7 @@ int up_image_special_to_gltf_pbr(up_context *ctx, const uint8_t *special, uint32
 
 int up_image_height_to_normal(up_context *ctx, const uint8_t *height_map, uint32_t width, uint32_t height, float strength, uint8_t *normal) {
 	if (!ctx || !height_map || !normal || width == 0 || height == 0 || !(strength == strength)) return UP_ERR_INVALID_ARGUMENT;
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_image_height_to_normal", [&]() {
 		set_device(ctx);
 		const size_t n = (size_t)width * height;
 		const uint8_t *hi = (const uint8_t *)stage_in(ctx, B_IN0, height_map, n);
@@ -673,7 +797,7 @@ int up_image_height_to_normal(up_context *ctx, const uint8_t *height_map, uint32
 int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta) {
 	if (!ctx || !points || !dL_dd || !dtheta || n == 0) return UP_ERR_INVALID_ARGUMENT;
 	if (!ctx->synthetic) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "the parameter adjoint needs a synthetic context");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_sdf_param_backward", [&]() {
 		set_device(ctx);
 		const size_t nt = up_synth_theta_count(&ctx->prog);
 		const float *dp = (const float *)stage_in(ctx, B_IN0, points, n * 12);
@@ -693,14 +817,15 @@ int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const 
 int up_sdf_param_backward_noalloc(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta) {
 	if (!ctx || !points || !dL_dd || !dtheta || n == 0) return UP_ERR_INVALID_ARGUMENT;
 	if (!ctx->synthetic) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "the parameter adjoint needs a synthetic context");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_sdf_param_backward_noalloc", [&]() {
 		set_device(ctx);
-		if (!is_device(points) || !is_device(dL_dd) || !is_device(dtheta))
+		if (!is_local(ctx, points) || !is_local(ctx, dL_dd) || !is_local(ctx, dtheta))
 			return fail(ctx, UP_ERR_INVALID_ARGUMENT,
-				"up_sdf_param_backward_noalloc needs device buffers: it allocates nothing, so it cannot stage host memory");
+				"up_sdf_param_backward_noalloc needs device buffers of the context's GPU: it allocates nothing, so it cannot stage "
+				"host memory or memory of another GPU");
 		if (up_synth_theta_count(&ctx->prog) > 43)
 			return fail(ctx, UP_ERR_INVALID_ARGUMENT, "parameter vector longer than the 43-entry scratch row");
-		check(launch_synth_bwd_noalloc(ctx->prog, points, n, dL_dd, dtheta, ctx->stream), "adjoint kernel (no allocation)");
+		check(launch_synth_bwd_noalloc(ctx->prog, points, n, dL_dd, dtheta, ctx->noalloc_scratch, ctx->stream), "adjoint kernel (no allocation)");
 		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
 		return (int)UP_OK;
 	});
@@ -712,7 +837,7 @@ int up_texture(up_context *ctx, int purpose, const up_mesh_in *mesh, uint32_t wi
 	if (!mesh->positions || !mesh->normals || !mesh->uvs || !mesh->indices || mesh->index_count % 3 != 0)
 		return fail(ctx, UP_ERR_INVALID_ARGUMENT, "mesh needs positions, normals, uvs and a multiple of 3 indices");
 	if ((uint64_t)width * height >= (1ull << 31)) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "atlas too large");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_texture", [&]() {
 		set_device(ctx);
 		const uint64_t V = mesh->vertex_count, I = mesh->index_count, n = (uint64_t)width * height;
 		const int ach = purpose == UP_PURPOSE_WATER ? 4 : 3;
@@ -747,7 +872,7 @@ int up_tiles(up_context *ctx, int purpose, const float *positions, const float *
 	if (!ctx || !positions || !normals || !out || n == 0) return UP_ERR_INVALID_ARGUMENT;
 	if (ctx->synthetic) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "tiles need a reference-mode context");
 	if (purpose < UP_PURPOSE_LAND || purpose > UP_PURPOSE_NAVIGATION) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "bad purpose");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_tiles", [&]() {
 		set_device(ctx);
 		const float *p = (const float *)stage_in(ctx, B_IN0, positions, n * 12);
 		const float *q = (const float *)stage_in(ctx, B_GRAD, normals, n * 12);
@@ -775,7 +900,7 @@ int up_batch_run(up_context *ctx, const up_synth_program *planets, size_t nplane
 		if (!valid_program(planets[i])) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "invalid planet program");
 	for (size_t c = 0; c < nchunks; c++)
 		if (chunks[c].planet >= nplanets || !valid_grid(&chunks[c].grid)) return fail(ctx, UP_ERR_INVALID_ARGUMENT, "invalid chunk");
-	return guarded(ctx, [&]() {
+	return guarded(ctx, "up_batch_run", [&]() {
 		set_device(ctx);
 		uint32_t ncells = 0, nquads = 0;
 		std::vector<uint32_t> cc, cq;
@@ -795,14 +920,11 @@ int up_batch_run(up_context *ctx, const up_synth_program *planets, size_t nplane
 		if (!out->positions || !out->indices || out->vertex_capacity < ncells || out->index_capacity < 6ull * nquads)
 			return fail(ctx, UP_ERR_CAPACITY, "batch output buffers too small");
 		if (out->values && out->values_capacity < nval) return fail(ctx, UP_ERR_CAPACITY, "batch values buffer too small");
-		const cudaMemcpyKind kp = is_device(out->positions) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-		check(cudaMemcpyAsync(out->positions, dpos, (size_t)ncells * 12, kp, ctx->stream), "cudaMemcpyAsync batch positions");
-		const cudaMemcpyKind ki = is_device(out->indices) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-		check(cudaMemcpyAsync(out->indices, didx, (size_t)nquads * 24, ki, ctx->stream), "cudaMemcpyAsync batch indices");
-		if (out->values) {
-			const cudaMemcpyKind kv = is_device(out->values) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-			check(cudaMemcpyAsync(out->values, dval, (size_t)nval * 4, kv, ctx->stream), "cudaMemcpyAsync batch values");
-		}
+		// host, this GPU or another GPU: unified addressing resolves the direction
+		check(cudaMemcpyAsync(out->positions, dpos, (size_t)ncells * 12, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync batch positions");
+		check(cudaMemcpyAsync(out->indices, didx, (size_t)nquads * 24, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync batch indices");
+		if (out->values)
+			check(cudaMemcpyAsync(out->values, dval, (size_t)nval * 4, cudaMemcpyDefault, ctx->stream), "cudaMemcpyAsync batch values");
 		check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
 		return (int)UP_OK;
 	});

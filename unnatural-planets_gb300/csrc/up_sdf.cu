@@ -12,7 +12,6 @@
 #include "up_grid_runs.cuh"
 #include <cmath>
 
-#include <mutex>
 
 namespace up {
 
@@ -480,40 +479,30 @@ static __device__ __align__(256) float g_noalloc_partials[NOALLOC_MAX_BLOCKS * A
 static const size_t NOALLOC_SCRATCH_BYTES = sizeof(float) * NOALLOC_MAX_BLOCKS * ACC_N;
 
 // Host code cannot pass g_noalloc_partials itself: in host code the name is a
-// host-side stand-in, not a device address. The device address is looked up
-// by the first call on each device (with that device current) and cached;
-// that first call should therefore come before any stream capture begins.
-static float *noalloc_scratch(int device, cudaError_t &err) {
-	constexpr int MAX_DEVICES = 64;
-	static std::mutex mu;
-	static float *addr[MAX_DEVICES] = {};
-	err = cudaSuccess;
-	if (device < 0 || device >= MAX_DEVICES) {
-		err = cudaErrorInvalidDevice;
-		return nullptr;
-	}
-	std::lock_guard<std::mutex> lock(mu);
-	if (!addr[device]) {
-		void *p = nullptr;
-		err = cudaGetSymbolAddress(&p, g_noalloc_partials);
-		if (err != cudaSuccess) return nullptr;
-		addr[device] = (float *)p;
-	}
-	return addr[device];
+// host-side stand-in, not a device address. Every context looks the device
+// address up once, at its creation (init_context in up_abi.cu, with the
+// context's device current), and passes it to each launch. Creating the
+// context also loads this file's module, so the array is resident from then
+// on, and no later call queries the runtime (a call inside a stream capture
+// makes no lookup). A device reset frees the array with everything else: the
+// contexts made before it are dead, and contexts made after it look the new
+// address up.
+cudaError_t noalloc_scratch_address(float **out) {
+	void *p = nullptr;
+	const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+	*out = e == cudaSuccess ? (float *)p : nullptr;
+	return e;
 }
 
 size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_BYTES; }
 int noalloc_max_blocks() { return NOALLOC_MAX_BLOCKS; }
 
-cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, cudaStream_t s) {
-	int dev = 0;
-	cudaError_t e = cudaGetDevice(&dev);
-	if (e != cudaSuccess) return e;
-	float *partials = noalloc_scratch(dev, e);
-	if (!partials) return e;
+cudaError_t launch_synth_bwd_noalloc(const up_synth_program &P, const float *xyz, uint64_t n, const float *w, float *dtheta, float *scratch,
+	cudaStream_t s) {
+	if (!scratch) return cudaErrorInvalidDevicePointer;
 	int nblocks = synth_bwd_blocks(n);
 	if (nblocks > NOALLOC_MAX_BLOCKS) nblocks = NOALLOC_MAX_BLOCKS;
-	return launch_synth_bwd(P, xyz, n, w, partials, nblocks, dtheta, s);
+	return launch_synth_bwd(P, xyz, n, w, scratch, nblocks, dtheta, s);
 }
 
 } // namespace up
