@@ -1,16 +1,18 @@
 """Writes up_sinnet_data.h: the weight tables of the two sine-network shapes
 (bunny, monkey head) of the reference's sources/sdf.cpp:252-290, read from
-the reference source tree (default /root/reference). The tables define the
-shapes, so they are kept alike; the header is committed and this recipe only
-regenerates it.
+the reference project's source tree, whose root is the one required argument.
+The tables define the shapes, so they are kept alike; the header is committed
+and this recipe only regenerates it.
 
-  python gen_sinnet_data.py [reference_root]
+  python gen_sinnet_data.py <reference_root>
 """
 import re
 import sys
 from pathlib import Path
 
-ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+if len(sys.argv) != 2:
+    sys.exit("usage: python gen_sinnet_data.py <reference_root>  (the root of the unnatural-planets source tree)")
+ROOT = Path(sys.argv[1])
 src = (ROOT / 'sources' / 'sdf.cpp').read_text()
 NUM = r'-?(?:\d+\.\d*|\.\d+|\d+)'
 def vec4s(s): return [[float(x) for x in re.findall(NUM, m)] for m in re.findall(r'Vec4\(([^)]*)\)', s)]
