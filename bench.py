@@ -54,6 +54,13 @@ CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit
 TRAFFIC_PER_SAMPLE_FUSED = 244.771584e6 / 16777216
 
 
+def workload_config(grid: int, n: int) -> dict:
+    """the config block of both arms' JSON lines (the same dict on both)"""
+    return {"workload": f"torus+8 spheres - ridged perlin 6 oct + cellular F2-F1, seed 42, {grid}^3 over [-1.6,1.6]^3",
+            "samples_per_step": grid ** 3, "parallelism": f"replicas x{n}",
+            "l2": "no inputs; 2.1 GB of outputs per step (> 129 MB L2)" if grid >= 512 else "no inputs"}
+
+
 def _pkg():
     return importlib.import_module("unnatural-planets_gb300")
 
@@ -380,14 +387,15 @@ def extra_fit(up, W, stream, steps=300):
     xg = AG.grid_positions(gg)  # the grid kernel's sample positions
     d_star = target.sdf_points(x, d=torch.empty(n, device="cuda"))
     s_star = torch.sign(target.sdf_points(xg, d=torch.empty(xg.shape[0], device="cuda")))
-    theta = torch.tensor(t0, device="cuda", requires_grad=True)
+    rel = AG.RelativeTheta(torch.tensor(t0, device="cuda"))   # theta = theta0 (1 + u), Adam moves u
     planet = up.Planet(program=W.torus_spheres_ridged_cellular())
     planet.set_stream(stream.cuda_stream)
-    opt = torch.optim.Adam([theta], lr=1e-2)
-    err0 = float((theta.detach() - t_star).norm() / t_star.norm())
+    opt = torch.optim.Adam(rel.parameters(), lr=1e-2)
+    err0 = float((rel().detach() - t_star).norm() / t_star.norm())
 
     def step():
         opt.zero_grad()
+        theta = rel()
         loss = ((AG.sdf(theta, x, planet) - d_star) ** 2).mean() + torch.relu(-AG.sdf_grid(theta, gg, planet, xg) * s_star).mean()
         loss.backward()
         opt.step()
@@ -401,7 +409,8 @@ def extra_fit(up, W, stream, steps=300):
     ms = 1e3 * (time.perf_counter() - t) / (steps - 1)
     # final SDF against the FP64 oracle at theta* on 65536 of the shell points
     xs = x[: 1 << 16].cpu().numpy()
-    planet.set_theta(theta.detach().cpu().numpy())
+    theta = rel().detach()
+    planet.set_theta(theta.cpu().numpy())
     fit = planet.sdf_points(xs)
     ref = O.synth_points(P, xs, theta=t_star_np.astype(np.float64))
     # relative error per parameter group (layout of workloads.theta_of)
@@ -422,7 +431,8 @@ def extra_fit(up, W, stream, steps=300):
             "sdf_rms_vs_fp64_oracle": float(np.sqrt(np.mean((fit - ref) ** 2))),
             "what": "torus + 8 spheres - ridged perlin + cellular, 25 parameters; theta* = theta (1 + 0.05 U) seed 1, "
                     "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell (Morton order) + "
-                    "mean(relu(-d sign(d*))) on 256^3 (forward through the grid kernel); Adam lr 1e-2; SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
+                    "mean(relu(-d sign(d*))) on 256^3 (forward through the grid kernel); Adam lr 1e-2 on the relative parameters u, "
+                    "theta = theta0 (1 + u); SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
 
 
 def extra_modes(up, stream):
@@ -483,7 +493,7 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded planet program; no dataset)",
-        "config": {"workload": f"torus+8 spheres - ridged perlin 6 oct + cellular F2-F1, seed 42, {args.grid}^3 over [-1.6,1.6]^3"},
+        "config": workload_config(args.grid, args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample, "cpu": _cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -632,9 +642,7 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_fused, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded planet program; no dataset)",
-        "config": {"workload": f"torus+8 spheres - ridged perlin 6 oct + cellular F2-F1, seed 42, {args.grid}^3 over [-1.6,1.6]^3",
-                   "samples_per_step": N, "parallelism": f"replicas x{ws}",
-                   "l2": "no inputs; 2.1 GB of outputs per step (> 129 MB L2)"},
+        "config": workload_config(args.grid, ws),
         "plain_gsamples_s": ws * N / (t_plain * 1e-3) / 1e9, "plain_ms": t_plain,
         "ms_per_planet": sum(planet_ms) / len(planet_ms),
         "ms_per_planet_full_grid": sum(planet_full_ms) / len(planet_full_ms),

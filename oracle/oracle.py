@@ -47,6 +47,7 @@ def lib(fast: bool = False) -> C.CDLL:
         "orc_synth_points": (None, [P, vp, vp, C.c_uint64, C.c_int, vp, vp, C.c_int]),
         "orc_synth_theta_grad": (C.c_int, [P, vp, vp, C.c_uint64, vp, vp, C.c_int]),
         "orc_synth_count_ops": (None, [P, vp, C.c_uint64, vp]),
+        "orc_synth_count_ops_grad": (None, [P, vp, C.c_uint64, vp]),
         "orc_synth_grid_fp32": (None, [P, G, C.c_uint32, C.c_uint32, vp, C.c_int]),
         "orc_synth_grid_fp32_cd": (None, [P, G, C.c_uint32, C.c_uint32, C.c_float, vp, vp, C.c_int]),
         "orc_grid_positions": (None, [G, vp]),
@@ -120,6 +121,15 @@ def synth_count_ops(P, xyz) -> dict:
     xyz = np.ascontiguousarray(xyz, np.float32)
     c = np.zeros(5, np.float64)
     lib().orc_synth_count_ops(C.byref(P), _p(xyz), xyz.shape[0], _p(c))
+    return dict(flop=c[0], div=c[1], sqrt=c[2], floor=c[3], transcendental=c[4])
+
+
+def synth_count_ops_grad(P, xyz) -> dict:
+    """operation counts per sample of the value with its gradient dd/dp
+    (sparse forward mode), same bins as synth_count_ops"""
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    c = np.zeros(5, np.float64)
+    lib().orc_synth_count_ops_grad(C.byref(P), _p(xyz), xyz.shape[0], _p(c))
     return dict(flop=c[0], div=c[1], sqrt=c[2], floor=c[3], transcendental=c[4])
 
 

@@ -150,6 +150,22 @@ void orc_synth_count_ops(const up_synth_program *prog, const float *xyz, uint64_
 	counts5[3] = (double)c.floor / n; counts5[4] = (double)c.transc / n;
 }
 
+// algorithmic operation counts per sample of the value together with its
+// gradient dd/dp (sparse forward mode over the counting scalar, CDual),
+// averaged over n points; same bins as orc_synth_count_ops
+void orc_synth_count_ops_grad(const up_synth_program *prog, const float *xyz, uint64_t n, double *counts5) {
+	const up_synth_program P = *prog;
+	auto th = theta_as<CDual>(P, nullptr);
+	opcounts() = OpCounts();
+	for (uint64_t i = 0; i < n; i++) {
+		const float *q = xyz + 3 * i;
+		(void)synth_eval(P, th.data(), V3<CDual>(CDual::var(q[0], 0), CDual::var(q[1], 1), CDual::var(q[2], 2)));
+	}
+	const OpCounts c = opcounts();
+	counts5[0] = (double)c.flop / n; counts5[1] = (double)c.div / n; counts5[2] = (double)c.sqrt / n;
+	counts5[3] = (double)c.floor / n; counts5[4] = (double)c.transc / n;
+}
+
 // ---------------------------------------------------------------- CPU baseline
 // The reference samples its SDF through a per-sample callback
 // (Delegate<Real(const Vec3&)>, sources/meshGeneration.cpp:39). The baseline

@@ -114,6 +114,75 @@ ORC_FL_T(sin) ORC_FL_T(cos) ORC_FL_T(atan) ORC_FL_T(acos) ORC_FL_T(log) ORC_FL_T
 template<bool C> inline Fl<C> pow(const Fl<C> &a, double p) { cnt<C>(&OpCounts::transc); Fl<C> r; r.v = std::pow(a.v, (float)p); return r; }
 template<bool C> inline Fl<C> atan2(const Fl<C> &y, const Fl<C> &x) { cnt<C>(&OpCounts::transc); Fl<C> r; r.v = std::atan2(y.v, x.v); return r; }
 
+// Forward-mode value + gradient over the counting FP32 scalar: the
+// algorithmic operation count of evaluating d and dd/dp together. A quantity
+// with a zero derivative (a constant, or anything computed only from
+// constants or from floor) carries no derivative lanes and costs nothing
+// extra, so the count is that of sparse forward-mode differentiation.
+struct CDual {
+	Counted v;
+	Counted d[3];
+	bool live = false;
+	CDual() = default;
+	CDual(double x) : v(x) {}
+	static CDual var(double x, int i) { CDual r(x); r.d[i] = Counted(1.0); r.live = true; return r; }
+};
+inline double val(const CDual &a) { return a.v.v; }
+inline CDual operator+(const CDual &a, const CDual &b) {
+	CDual r; r.v = a.v + b.v; r.live = a.live || b.live;
+	for (int i = 0; i < 3; i++) r.d[i] = a.live && b.live ? a.d[i] + b.d[i] : (a.live ? a.d[i] : b.d[i]);
+	return r;
+}
+inline CDual operator-(const CDual &a) {
+	CDual r; r.v = -a.v; r.live = a.live;
+	for (int i = 0; a.live && i < 3; i++) r.d[i] = -a.d[i];
+	return r;
+}
+inline CDual operator-(const CDual &a, const CDual &b) {
+	CDual r; r.v = a.v - b.v; r.live = a.live || b.live;
+	for (int i = 0; i < 3; i++) r.d[i] = a.live && b.live ? a.d[i] - b.d[i] : (a.live ? a.d[i] : (b.live ? -b.d[i] : Counted()));
+	return r;
+}
+inline CDual operator*(const CDual &a, const CDual &b) {
+	CDual r; r.v = a.v * b.v; r.live = a.live || b.live;
+	for (int i = 0; i < 3; i++)
+		r.d[i] = a.live && b.live ? a.d[i] * b.v + a.v * b.d[i] : (a.live ? a.d[i] * b.v : (b.live ? a.v * b.d[i] : Counted()));
+	return r;
+}
+inline CDual cd_chain(const CDual &a, Counted v, Counted dv) {
+	CDual r; r.v = v; r.live = a.live;
+	for (int i = 0; a.live && i < 3; i++) r.d[i] = a.d[i] * dv;
+	return r;
+}
+inline CDual operator/(const CDual &a, const CDual &b) {
+	CDual r; r.v = a.v / b.v; r.live = a.live || b.live;
+	if (!r.live) return r;
+	const Counted inv = Counted(1.0) / b.v;
+	for (int i = 0; i < 3; i++) {
+		if (a.live && b.live) r.d[i] = (a.d[i] - r.v * b.d[i]) * inv;
+		else if (a.live) r.d[i] = a.d[i] * inv;
+		else r.d[i] = -(r.v * b.d[i]) * inv;
+	}
+	return r;
+}
+#define ORC_CD_MIX(OP) \
+	inline CDual operator OP(const CDual &a, double b) { return a OP CDual(b); } \
+	inline CDual operator OP(double a, const CDual &b) { return CDual(a) OP b; }
+ORC_CD_MIX(+) ORC_CD_MIX(-) ORC_CD_MIX(*) ORC_CD_MIX(/)
+#undef ORC_CD_MIX
+inline CDual &operator+=(CDual &a, const CDual &b) { a = a + b; return a; }
+inline CDual &operator-=(CDual &a, const CDual &b) { a = a - b; return a; }
+inline CDual &operator*=(CDual &a, const CDual &b) { a = a * b; return a; }
+inline CDual &operator/=(CDual &a, const CDual &b) { a = a / b; return a; }
+inline CDual sqrt(const CDual &a) { const Counted s = sqrt(a.v); return cd_chain(a, s, a.live ? Counted(0.5) / s : Counted()); }
+inline CDual abs(const CDual &a) {
+	CDual r; r.v = abs(a.v); r.live = a.live;
+	for (int i = 0; a.live && i < 3; i++) r.d[i] = val(a) < 0 ? -a.d[i] : a.d[i];
+	return r;
+}
+inline CDual floor(const CDual &a) { CDual r; r.v = floor(a.v); return r; }
+inline void count_sel(const CDual &) { cnt<true>(&OpCounts::flop); }
+
 using std::sqrt; using std::floor; using std::sin; using std::cos; using std::atan; using std::acos;
 using std::log; using std::exp; using std::atan2; using std::pow;
 inline double abs(double x) { return std::fabs(x); }

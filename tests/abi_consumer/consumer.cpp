@@ -1,5 +1,5 @@
 // A C++ consumer of include/up_abi.h written the way the reference would bind
-// it (the snippets of INTEGRATION.md made into one program): mode selection by
+// it (the binding a reference maintainer would write, as one program): mode selection by
 // name, the per-point terrain callbacks called from several threads at once
 // (generator.cpp:159,215,432-439 run the land, water and navmesh pipelines
 // concurrently), the base land mesh with the capacity protocol, texels of a

@@ -1,6 +1,6 @@
 """include/up_abi.h as the reference would use it: a C++17 program (the
-INTEGRATION.md snippets made into one, with the terrain callbacks called from
-eight threads at once) and a C99 program, both compiled with the system
+binding a reference maintainer would write, made into one program, with the
+terrain callbacks called from eight threads at once) and a C99 program, both compiled with the system
 compilers against the header and linked to libup_gb300.so. The CPU tests
 compile and link them (and the header alone as C and as C++ with warnings as
 errors); the GPU test runs them."""

@@ -1,15 +1,21 @@
 """GPU parity of the reference modes (34 shapes, 6 elevation modes, 5
 fields) through the C ABI.
 
-Tolerances: the CUDA path and the per-operation FP32 oracle agree within
-1e-4 * max(1, |d|) for at least 99.5% of the samples (the remainder sits on
-discontinuities of the reference formulas: Mandelbulb escape counts, gear
-sectors, Voronoi cells, cellular swaps). Against FP64 the same bound holds
-for 98% of the samples: FP32 itself loses digits in some reference formulas
-(sin/cos of arguments near 300 in "fibers", frequency-1 noise at Voronoi
-points in "craters"), which the reference's own FP32 code shares.
-Gradients are checked against the FP64 forward-mode oracle away from those
-discontinuities (99%)."""
+Tolerances (the benchmark spec: SDF error <= 1e-5 relative to the FP64 oracle, taken
+relative to the planets' shape scale, the sphere radius R = 1100 of
+sdf.cpp:20-23, so 0.011 in the planets' units):
+  - against FP64, at least 99.9 % of the samples of every shape and every
+    elevation field are within 1e-5 R (measured on GB300: every shape has no
+    sample beyond it except "mandelbulb", whose FP32 escape counts flip on
+    5e-4 of the samples);
+  - named exception: the raw elevation of "craters" (field ELEVATION_RAW)
+    loses digits in FP32 itself (frequency-1 noise evaluated at Voronoi
+    points); it is held to the same bound against the per-operation FP32
+    oracle, and against FP64 only to 1e-4 R;
+  - against the per-operation FP32 oracle the same 1e-5 R bound holds for
+    99.9 % of the samples everywhere.
+Gradients are checked against the FP64 forward-mode oracle away from the
+formulas' discontinuities (99%)."""
 from __future__ import annotations
 
 import numpy as np
@@ -30,8 +36,17 @@ def _pts(n=4000, seed=0):
     return np.random.default_rng(seed).uniform(-2000, 2000, size=(n, 3)).astype(np.float32)
 
 
+R_SCALE = 1100.0          # the reference planets' shape scale (sdf.cpp:20-23)
+TOL = 1e-5 * R_SCALE
+
+
 def _rel(a, b):
     return np.abs(np.asarray(a, np.float64) - b) / np.maximum(1.0, np.abs(b))
+
+
+def _beyond(a, b, tol=TOL):
+    """fraction of samples with |a - b| > tol (planet units)"""
+    return (np.abs(np.asarray(a, np.float64) - b) > tol).mean()
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -42,8 +57,8 @@ def test_shapes_water_field(cuda, up, O, shape):
     ref = O.Planet(shape, "none", seed=11)
     f32 = ref.field(1, x, precision=1)
     f64, g64 = ref.field(1, x, grad=True)
-    assert (_rel(d, f32) > 1e-4).mean() <= 5e-3
-    assert (_rel(d, f64) > 1e-4).mean() <= 2e-2
+    assert _beyond(d, f32) <= 1e-3, _beyond(d, f32)
+    assert _beyond(d, f64) <= 1e-3, _beyond(d, f64)
     ge = np.abs(g - g64).max(axis=1) / np.maximum(1.0, np.abs(g64).max(axis=1))
     assert (ge > 1e-3).mean() <= 1e-2
 
@@ -55,8 +70,11 @@ def test_elevation_fields(cuda, up, O, elev, field):
     planet = up.Planet("sphere", elev, seed=5)
     d = planet.sdf_points(x, field=field)
     ref = O.Planet("sphere", elev, seed=5)
-    assert (_rel(d, ref.field(field, x, precision=1)) > 1e-4).mean() <= 5e-3
-    assert (_rel(d, ref.field(field, x)) > 1e-4).mean() <= 2e-2
+    assert _beyond(d, ref.field(field, x, precision=1)) <= 1e-3
+    if elev == "craters" and field == 4:   # FP32 itself is the limit (see the module docstring)
+        assert _beyond(d, ref.field(field, x), tol=10 * TOL) <= 1e-3
+    else:
+        assert _beyond(d, ref.field(field, x)) <= 1e-3
 
 
 def test_three_fields_in_one_pass(cuda, up, O):
@@ -89,20 +107,25 @@ def test_invalid_modes(cuda, up):
     assert up.Planet("bowl", "none").double_sided and not up.Planet("sphere", "none").double_sided
 
 
-def test_mode_contour_matches_oracle(cuda, up, O):
-    """Land contour of sphere/lakes at 48^3 over the reference box (+-2000):
-    bit-exact topology against the oracle's contouring of the same grid."""
-    g = up.abi.Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), (48, 48, 48))
-    planet = up.Planet("sphere", "lakes", seed=4)
+@pytest.mark.parametrize("shape,elevation,seed,n", [("sphere", "lakes", 4, 96), ("torus", "islands", 2, 64), ("h2o", "craters", 5, 64),
+                                                   ("box", "legacy", 6, 64)])
+def test_mode_contour_matches_oracle(cuda, up, O, shape, elevation, seed, n):
+    """Land contour of reference-mode planets over the reference box (+-2000):
+    bit-exact topology against the oracle's contouring of the same grid;
+    vertices within 1e-3 of a cell for 99.9 % of them. The lakes/mountains
+    formulas have gradient kinks (saturate, max, terrace, smoothMax) where a
+    Hermite normal may come from either side: measured on GB300, 0.045 % of
+    the sphere/lakes vertices at 96^3 (0.24 % at 48^3, whose cells straddle
+    more kinks), none for the other planets."""
+    g = up.abi.Grid.make((-2000, -2000, -2000), (2000, 2000, 2000), (n, n, n))
+    planet = up.Planet(shape, elevation, seed=seed)
     d = planet.sdf_grid(g, 1)[0]
     pos, nrm, idx = planet.contour(g, field=0, values=d)
-    ref = O.Planet("sphere", "lakes", seed=4).contour(0, g, d)
+    ref = O.Planet(shape, elevation, seed=seed).contour(0, g, d)
     assert np.array_equal(idx, ref["indices"])
-    step = 4000.0 / 47
+    step = 4000.0 / (n - 1)
     err = np.abs(pos - ref["positions"]).max(axis=1) / step
-    # the lakes/mountains formulas have gradient kinks (saturate, max, terrace,
-    # smoothMax): Hermite normals taken there may come from either side
-    assert (err > 1e-3).mean() <= 1e-2 and err.max() <= 1.0
+    assert (err > 1e-3).mean() <= 1e-3 and err.max() <= 1.0
 
 
 @pytest.mark.parametrize("shape,elevation,seed", [("sphere", "lakes", 1), ("torus", "islands", 2), ("cube", "simple", 3),
@@ -142,4 +165,4 @@ def test_modes_grid_runs_kernel(cuda, up, O, shape, elevation, seed):
             if not (mask >> f) & 1:
                 continue
             assert (_rel(outs[f], pts[f]) > 1e-5).mean() <= 1e-3, (mask, f)
-            assert (_rel(outs[f], ref.field(f, pos, precision=1)) > 1e-4).mean() <= 5e-3, (mask, f)
+            assert _beyond(outs[f], ref.field(f, pos, precision=1)) <= 1e-3, (mask, f)

@@ -149,3 +149,18 @@ def test_flop_count_constant(O):
     x = np.random.default_rng(0).uniform(-1.6, 1.6, size=(20000, 3)).astype(np.float32)
     c = O.synth_count_ops(W.torus_spheres_ridged_cellular(), x)
     assert abs(c["flop"] - W.FLOPS_PER_SAMPLE_C2) / W.FLOPS_PER_SAMPLE_C2 < 0.01
+    # value with gradient, sparse forward mode over the same counting scalar
+    cg = O.synth_count_ops_grad(W.torus_spheres_ridged_cellular(), x)
+    assert abs(cg["flop"] - W.FLOPS_PER_SAMPLE_C2_FWD_GRAD) / W.FLOPS_PER_SAMPLE_C2_FWD_GRAD < 0.01
+    assert cg["sqrt"] == c["sqrt"] and cg["floor"] == c["floor"]
+
+
+def test_forward_mode_count_exceeds_value_count(O):
+    """Each operation on a quantity that depends on p also updates three
+    derivative lanes, so the value-with-gradient count of the plain method is
+    more than three times its value count."""
+    W = workloads()
+    P = W.sphere_fbm()
+    x = np.random.default_rng(3).uniform(-1.3, 1.3, size=(500, 3)).astype(np.float32)
+    c = O.synth_count_ops_grad(P, x)
+    assert c["flop"] > 3 * O.synth_count_ops(P, x)["flop"]

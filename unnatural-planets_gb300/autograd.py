@@ -76,6 +76,24 @@ def grid_positions(grid, device="cuda") -> torch.Tensor:
     return torch.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], dim=1).contiguous()
 
 
+class RelativeTheta(torch.nn.Module):
+    """theta = theta0 * (1 + u), with u the parameter an optimiser moves.
+
+    The program's parameters span five orders of magnitude (octave amplitudes
+    of 6e-4, frequencies up to 96, radii near 1). An optimiser step of fixed
+    size in theta overshoots the small ones and barely moves the large ones;
+    in u every parameter moves in units of its own starting size. Entries of
+    theta0 that are 0 cannot move."""
+
+    def __init__(self, theta0: torch.Tensor):
+        super().__init__()
+        self.register_buffer("theta0", theta0.detach().clone())
+        self.u = torch.nn.Parameter(torch.zeros_like(self.theta0))
+
+    def forward(self) -> torch.Tensor:
+        return self.theta0 * (1 + self.u)
+
+
 def _theta_of(planet):
     from .workloads import theta_of
     return theta_of(planet.program)

@@ -6,7 +6,7 @@
 // CPU tasks (tasksRunBlocking, sources/generator.cpp:159,215).
 //
 // Stages (each one launch covering every chunk):
-//   sample  persistent blocks pull 4096-sample tiles from a device work
+//   sample  persistent blocks pull tiles of samples from a device work
 //           counter; a tile belongs to one chunk (binary search of the tile
 //           table); values go to one concatenated grid, and the sign bits
 //           of every chunk, 32 points per word, to chunk c's words from
@@ -18,10 +18,12 @@
 //   emit    ordered lists and per-chunk maps
 //   hermite / qef / quads  over the global lists, chunk found by binary search
 // The first call for a given (planets, chunks) input runs eagerly (the host
-// needs the totals to size the lists), autotunes the sampling block size
-// among 128/256/512 threads, then captures the stages in a CUDA graph on a
-// private stream; later calls with byte-identical inputs replay the graph
-// (the same work, recomputed) without host round trips.
+// needs the totals to size the lists), autotunes the sampling stage's tile
+// shape (1024 to 16384 samples per tile) and block size (128/256/512
+// threads) by timing each pair on this input, then captures the stages in a
+// CUDA graph on a private stream; later calls with byte-identical inputs
+// replay the graph (the same work, recomputed, with the chosen shape) without
+// host round trips.
 #include "up_contour.cuh"
 #include "up_synth.cuh"
 
@@ -33,13 +35,17 @@ namespace up {
 struct BatchChunkDev {
 	GridDev g;
 	uint32_t planet;
-	uint32_t pt_off, cell_off, blk_off, tile_off;
+	uint32_t pt_off, cell_off, blk_off;
 	uint32_t word_off, nwords; // sign words: ceil(points / 32) + 2 (zero slack for dc_bits_at)
 	float band; // narrow band of contouring (0: exact values, when the caller reads them)
 	FastDiv divx, divy; // by n[0] and n[1]
 };
 
-constexpr uint32_t BATCH_TILE = 4096; // timed against 1024 to 16384 samples
+// tile shapes of the sampling stage, chosen per input by the autotune
+constexpr int BATCH_NTILE = 5;
+constexpr uint32_t BATCH_TILES[BATCH_NTILE] = {1024, 2048, 4096, 8192, 16384};
+// dynamic shared memory of a tile: its list of band samples and its sign words
+__host__ __device__ constexpr size_t batch_tile_smem(uint32_t tile) { return (size_t)tile * 2 + (size_t)tile / 32 * 4; }
 
 __device__ __forceinline__ uint32_t find_chunk(const uint32_t *__restrict__ starts, uint32_t n, uint32_t x) {
 	// last c with starts[c] <= x (starts ascending, starts[0] = 0)
@@ -72,11 +78,12 @@ __device__ __forceinline__ float batch_eval(const up_synth_program &P, V3f p) {
 // first pass) are formed in shared memory and stored with the values.
 template<int THREADS>
 __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_program *__restrict__ planets, const BatchChunkDev *__restrict__ chunks,
-	const uint32_t *__restrict__ tile_starts, uint32_t nchunks, uint32_t ntiles, float *__restrict__ d, uint32_t *__restrict__ bits,
+	const uint32_t *__restrict__ tile_starts, uint32_t nchunks, uint32_t ntiles, uint32_t TILE, float *__restrict__ d, uint32_t *__restrict__ bits,
 	unsigned *__restrict__ counter, unsigned *__restrict__ nanflag) {
 	__shared__ uint32_t tile, nnear;
-	__shared__ uint16_t near[BATCH_TILE];
-	__shared__ uint32_t words[BATCH_TILE / 32];
+	extern __shared__ uint32_t batch_smem[]; // TILE / 32 sign words, then TILE list entries
+	uint32_t *words = batch_smem;
+	uint16_t *near = (uint16_t *)(batch_smem + TILE / 32);
 	const uint32_t lane = threadIdx.x & 31;
 	bool bad = false;
 	for (;;) {
@@ -89,10 +96,10 @@ __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_pr
 		const up_synth_program &P = planets[ch.planet];
 		const uint32_t nx = ch.g.n[0], ny = ch.g.n[1];
 		const uint32_t npts = nx * ny * ch.g.n[2];
-		const uint32_t base = (t - ch.tile_off) * BATCH_TILE;
+		const uint32_t base = (t - tile_starts[c]) * TILE;
 		const FastDiv dx = ch.divx, dy = ch.divy;
 		#pragma unroll 1
-		for (uint32_t it = threadIdx.x; it < BATCH_TILE; it += THREADS) { // every thread the same trip count
+		for (uint32_t it = threadIdx.x; it < TILE; it += THREADS) { // every thread the same trip count
 			const uint32_t s = base + it;
 			bool full = false, neg = false;
 			if (s < npts) {
@@ -133,10 +140,11 @@ __global__ void __launch_bounds__(THREADS) batch_sample_kernel(const up_synth_pr
 		// the tile's words that belong to the chunk (its data words, and the
 		// two zero words after them from its last tile)
 		const uint32_t w0 = base >> 5;
-		if (threadIdx.x < BATCH_TILE / 32 && w0 + threadIdx.x < ch.nwords) bits[ch.word_off + w0 + threadIdx.x] = words[threadIdx.x];
-		if (threadIdx.x < 2 && base + BATCH_TILE >= npts) {
+		for (uint32_t w = threadIdx.x; w < TILE / 32; w += THREADS)
+			if (w0 + w < ch.nwords) bits[ch.word_off + w0 + w] = words[w];
+		if (threadIdx.x < 2 && base + TILE >= npts) {
 			const uint32_t ws = (npts + 31) / 32 + threadIdx.x; // slack words
-			if (ws >= w0 + BATCH_TILE / 32) bits[ch.word_off + ws] = 0u;
+			if (ws >= w0 + TILE / 32) bits[ch.word_off + ws] = 0u;
 		}
 		__syncthreads(); // the tile's list and words are read before the next tile is taken
 	}
@@ -294,9 +302,11 @@ struct DevBuf {
 
 struct BatchState {
 	std::vector<uint8_t> key;      // bytes of (planets, chunks) of the planned input
-	uint32_t nchunks = 0, npts = 0, ncells_all = 0, nblocks = 0, ntiles = 0;
+	uint32_t nchunks = 0, npts = 0, ncells_all = 0, nblocks = 0;
 	uint32_t ncells = 0, nedges = 0, nquads = 0;
 	int threads = 256;             // autotuned sampling block size
+	int tile_sel = 2;              // autotuned tile shape: BATCH_TILES[tile_sel]
+	uint32_t ntiles_of[BATCH_NTILE] = {}; // tiles of the whole input per tile shape
 	uint32_t nwords = 0;
 	DevBuf planets, chunks, tiles, blkst, grid, signs, blk, totals, off, cmap, emap, clist, elist, qlist, et, en, pos, idx, counter, flag, fb;
 	cudaStream_t stream = nullptr;
@@ -309,26 +319,31 @@ struct BatchState {
 	}
 };
 
-static int sample_blocks(int threads) {
-	const void *k = threads == 128 ? (const void *)batch_sample_kernel<128> : (threads == 512 ? (const void *)batch_sample_kernel<512> : (const void *)batch_sample_kernel<256>);
-	return persistent_blocks(k, threads);
+static const void *sample_kernel(int threads) {
+	return threads == 128 ? (const void *)batch_sample_kernel<128> : (threads == 512 ? (const void *)batch_sample_kernel<512> : (const void *)batch_sample_kernel<256>);
 }
 
-static cudaError_t enqueue_sample(BatchState &S, int threads, cudaStream_t s) {
+// the sampling stage with block size `threads` and tile shape BATCH_TILES[ts]
+// (tile table ts of S.tiles)
+static cudaError_t enqueue_sample(BatchState &S, int threads, int ts, cudaStream_t s) {
 	cudaError_t e = cudaMemsetAsync(S.counter.p, 0, 4, s);
 	if (e != cudaSuccess) return e;
-	const int b = sample_blocks(threads);
+	const uint32_t tile = BATCH_TILES[ts];
+	const size_t smem = batch_tile_smem(tile);
+	const int b = persistent_blocks(sample_kernel(threads), threads, smem);
 	const auto *P = S.planets.as<up_synth_program>();
 	const auto *C = S.chunks.as<BatchChunkDev>();
+	const uint32_t *T = S.tiles.as<uint32_t>() + (size_t)ts * S.nchunks;
 	uint32_t *B = S.signs.as<uint32_t>();
-	if (threads == 128) batch_sample_kernel<128><<<b, 128, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
-	else if (threads == 512) batch_sample_kernel<512><<<b, 512, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
-	else batch_sample_kernel<256><<<b, 256, 0, s>>>(P, C, S.tiles.as<uint32_t>(), S.nchunks, S.ntiles, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	const uint32_t nt = S.ntiles_of[ts];
+	if (threads == 128) batch_sample_kernel<128><<<b, 128, smem, s>>>(P, C, T, S.nchunks, nt, tile, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	else if (threads == 512) batch_sample_kernel<512><<<b, 512, smem, s>>>(P, C, T, S.nchunks, nt, tile, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
+	else batch_sample_kernel<256><<<b, 256, smem, s>>>(P, C, T, S.nchunks, nt, tile, S.grid.as<float>(), B, S.counter.as<unsigned>(), S.flag.as<unsigned>());
 	return cudaGetLastError();
 }
 
 static cudaError_t enqueue_front(BatchState &S, cudaStream_t s) {
-	cudaError_t e = enqueue_sample(S, S.threads, s);
+	cudaError_t e = enqueue_sample(S, S.threads, S.tile_sel, s);
 	if (e != cudaSuccess) return e;
 	batch_count_kernel<<<S.nblocks, DC_T, 0, s>>>(S.signs.as<uint32_t>(), S.chunks.as<BatchChunkDev>(), S.blkst.as<uint32_t>(), S.nchunks, S.nblocks, S.blk.as<uint32_t>());
 	if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -401,8 +416,8 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		if ((e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)) != cudaSuccess) return e;
 		// host chunk table
 		std::vector<BatchChunkDev> tab(nchunks);
-		std::vector<uint32_t> tiles(nchunks), blks(nchunks);
-		uint64_t pts = 0, cells = 0, nb = 0, nt = 0, nw = 0;
+		std::vector<uint32_t> tiles((size_t)BATCH_NTILE * nchunks), blks(nchunks);
+		uint64_t pts = 0, cells = 0, nb = 0, nw = 0, nt[BATCH_NTILE] = {};
 		for (size_t c = 0; c < nchunks; c++) {
 			BatchChunkDev &t = tab[c];
 			t.g = make_grid(chunks[c].grid);
@@ -414,23 +429,25 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 			t.pt_off = (uint32_t)pts;
 			t.cell_off = (uint32_t)cells;
 			t.blk_off = (uint32_t)nb;
-			t.tile_off = (uint32_t)nt;
 			t.word_off = (uint32_t)nw;
 			t.nwords = (uint32_t)((n + 31) / 32 + 2);
-			tiles[c] = t.tile_off;
+			for (int ts = 0; ts < BATCH_NTILE; ts++) { // first tile of chunk c per tile shape
+				tiles[(size_t)ts * nchunks + c] = (uint32_t)nt[ts];
+				nt[ts] += (n + BATCH_TILES[ts] - 1) / BATCH_TILES[ts];
+			}
 			blks[c] = t.blk_off;
 			pts += n;
 			cells += (uint64_t)(t.g.n[0] - 1) * (t.g.n[1] - 1) * (t.g.n[2] - 1);
 			nb += (n + DC_WPB - 1) / DC_WPB;
-			nt += (n + BATCH_TILE - 1) / BATCH_TILE;
 			nw += t.nwords;
 		}
 		if (3 * pts >= (1ull << 32)) return cudaErrorInvalidValue;
-		S->nchunks = (uint32_t)nchunks; S->npts = (uint32_t)pts; S->ncells_all = (uint32_t)cells; S->nblocks = (uint32_t)nb; S->ntiles = (uint32_t)nt;
+		S->nchunks = (uint32_t)nchunks; S->npts = (uint32_t)pts; S->ncells_all = (uint32_t)cells; S->nblocks = (uint32_t)nb;
+		for (int ts = 0; ts < BATCH_NTILE; ts++) S->ntiles_of[ts] = (uint32_t)nt[ts];
 		S->nwords = (uint32_t)nw;
 		if ((e = S->planets.ensure(nplanets * sizeof(up_synth_program))) != cudaSuccess) return e;
 		if ((e = S->chunks.ensure(nchunks * sizeof(BatchChunkDev))) != cudaSuccess) return e;
-		if ((e = S->tiles.ensure(nchunks * 4)) != cudaSuccess) return e;
+		if ((e = S->tiles.ensure(tiles.size() * 4)) != cudaSuccess) return e;
 		if ((e = S->blkst.ensure(nchunks * 4)) != cudaSuccess) return e;
 		if ((e = S->signs.ensure(nw * 4)) != cudaSuccess) return e;
 		if ((e = S->grid.ensure(pts * 4)) != cudaSuccess) return e;
@@ -449,27 +466,30 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 		cudaEventDestroy(ev);
 		cudaMemcpyAsync(S->planets.p, planets, nplanets * sizeof(up_synth_program), cudaMemcpyHostToDevice, s);
 		cudaMemcpyAsync(S->chunks.p, tab.data(), nchunks * sizeof(BatchChunkDev), cudaMemcpyHostToDevice, s);
-		cudaMemcpyAsync(S->tiles.p, tiles.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
+		cudaMemcpyAsync(S->tiles.p, tiles.data(), tiles.size() * 4, cudaMemcpyHostToDevice, s);
 		cudaMemcpyAsync(S->blkst.p, blks.data(), nchunks * 4, cudaMemcpyHostToDevice, s);
 		cudaMemsetAsync(S->flag.p, 0, 4, s);
-		// autotune the sampling block size (each candidate runs the full
-		// sampling stage once, after one untimed run that warms the caches)
+		// autotune the sampling stage's tile shape and block size: each
+		// (tile, threads) candidate runs the full sampling stage of this input
+		// once, after one untimed run that warms the caches; the fastest is
+		// kept for this input's plan and its graph
 		{
 			cudaEvent_t a, b;
 			cudaEventCreate(&a);
 			cudaEventCreate(&b);
 			float best = 1e30f;
-			e = enqueue_sample(*S, 256, s);
-			for (int t : {128, 256, 512}) {
-				if (e != cudaSuccess) break;
-				cudaEventRecord(a, s);
-				if ((e = enqueue_sample(*S, t, s)) != cudaSuccess) break;
-				cudaEventRecord(b, s);
-				cudaEventSynchronize(b);
-				float ms = 0.f;
-				cudaEventElapsedTime(&ms, a, b);
-				if (ms < best) { best = ms; S->threads = t; }
-			}
+			e = enqueue_sample(*S, 256, 2, s);
+			for (int ts = 0; ts < BATCH_NTILE && e == cudaSuccess; ts++)
+				for (int t : {128, 256, 512}) {
+					if (e != cudaSuccess) break;
+					cudaEventRecord(a, s);
+					if ((e = enqueue_sample(*S, t, ts, s)) != cudaSuccess) break;
+					cudaEventRecord(b, s);
+					cudaEventSynchronize(b);
+					float ms = 0.f;
+					cudaEventElapsedTime(&ms, a, b);
+					if (ms < best) { best = ms; S->threads = t; S->tile_sel = ts; }
+				}
 			cudaEventDestroy(a);
 			cudaEventDestroy(b);
 			if (e != cudaSuccess) return e;

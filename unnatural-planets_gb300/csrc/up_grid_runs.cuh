@@ -107,11 +107,20 @@ UP_HD void acc_add(Acc4 *a, int i, float v, float gx, float gy, float gz) {
 	a[i] = t;
 }
 UP_HD void acc_add(float *a, int i, float v, float, float, float) { a[i] += v; }
+// value term a * b added with one rounding (fmaf), on the device and the host
+// alike, so the value-only and value+gradient forms agree bit for bit
+UP_HD void acc_add_fma(Acc4 *acc, int i, float a, float b, float gx, float gy, float gz) {
+	Acc4 t = acc[i];
+	t.v = fmaf(a, b, t.v); t.gx += gx; t.gy += gy; t.gz += gz;
+	acc[i] = t;
+}
+UP_HD void acc_add_fma(float *acc, int i, float a, float b, float, float, float) { acc[i] = fmaf(a, b, acc[i]); }
 
 // one octave of lattice noise (VALUE = value noise, else Perlin); subtracts
 // amp * s(n) (s = n or 1 - 2|n|) from every sample of the run
-template<bool GRAD, bool VALUE>
-UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
+// RIDGED is a compile-time flag: the per-sample loop carries no branch on it
+template<bool GRAD, bool VALUE, bool RIDGED>
+UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
 	const float qy = rc.py * f, qz = rc.pz * f;
 	const float fy0 = floorf(qy), fz0 = floorf(qz);
 	const int iy = (int)fy0, iz = (int)fz0;
@@ -155,27 +164,28 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 				const uint32_t hh = mix32(xh ^ yz[c]);
 				cg[c] = VALUE ? v3(hash_signed(hh), 0.f, 0.f) : grad_lookup(hh);
 			}
-			float gxs = 0.f, cs = 0.f, pys = 0.f, qys = 0.f, pzs = 0.f, qzs = 0.f;
+			// the face's coefficients, summed over its 4 corners in pairs:
+			// (GX, C) += W (g.x, cyz); (Py, Pz) += (dWy, dWz) g.x;
+			// (Qy, Qz) += W (g.y, g.z) + (dWy, dWz) cyz
+			P2 gc = p2(0.f, 0.f), pyz = p2(0.f, 0.f), qyz = p2(0.f, 0.f);
 			#pragma unroll
 			for (int c = 0; c < 4; c++) {
+				const P2 dW = p2(dWy[c], dWz[c]);
 				if (VALUE) {
 					const float val = cg[c].x;
-					cs += Wyz[c] * val;
-					if (GRAD) { qys += dWy[c] * val; qzs += dWz[c] * val; }
+					gc.y += Wyz[c] * val;
+					if (GRAD) qyz = fma2(dW, p2s(val), qyz);
 				} else {
 					const V3f g = cg[c];
 					const float cyz = g.y * ys[c] + g.z * zs[c];
-					gxs += Wyz[c] * g.x;
-					cs += Wyz[c] * cyz;
+					gc = fma2(p2s(Wyz[c]), p2(g.x, cyz), gc);
 					if (GRAD) {
-						pys += dWy[c] * g.x;
-						qys += dWy[c] * cyz + Wyz[c] * g.y;
-						pzs += dWz[c] * g.x;
-						qzs += dWz[c] * cyz + Wyz[c] * g.z;
+						pyz = fma2(dW, p2s(g.x), pyz);
+						qyz = fma2(dW, p2s(cyz), fma2(p2s(Wyz[c]), p2(g.y, g.z), qyz));
 					}
 				}
 			}
-			GX[h] = gxs; Cc[h] = cs; Py[h] = pys; Qy[h] = qys; Pz[h] = pzs; Qz[h] = qzs;
+			GX[h] = gc.x; Cc[h] = gc.y; Py[h] = pyz.x; Qy[h] = qyz.x; Pz[h] = pyz.y; Qz[h] = qyz.y;
 		}
 		#pragma unroll 1
 		for (; r < R; r++) {
@@ -188,19 +198,24 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 			const float dA = A1 - A0;
 			const float n = A0 + u * dA;
 			float s = n, ds = 1.f;
-			if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
+			if (RIDGED) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
 			if (GRAD) {
 				const float du = e.du;
 				const float dnx = (VALUE ? 0.f : GX[0] + u * (GX[1] - GX[0])) + du * dA;
 				const float y0v = VALUE ? Qy[0] : fx * Py[0] + Qy[0], y1v = VALUE ? Qy[1] : (fx - 1.f) * Py[1] + Qy[1];
 				const float z0v = VALUE ? Qz[0] : fx * Pz[0] + Qz[0], z1v = VALUE ? Qz[1] : (fx - 1.f) * Pz[1] + Qz[1];
 				const float k = -amp * ds * f;
-				acc_add(acc, r * stride, -amp * s, k * dnx, k * (y0v + u * (y1v - y0v)), k * (z0v + u * (z1v - z0v)));
+				acc_add_fma(acc, r * stride, -amp, s, k * dnx, k * (y0v + u * (y1v - y0v)), k * (z0v + u * (z1v - z0v)));
 			} else {
-				acc_add(acc, r * stride, -amp * s, 0.f, 0.f, 0.f);
+				acc_add_fma(acc, r * stride, -amp, s, 0.f, 0.f, 0.f);
 			}
 		}
 	}
+}
+template<bool GRAD, bool VALUE>
+UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
+	if (ridged) lattice_octave_run_t<GRAD, VALUE, true>(rc, R, f, amp, key, acc, stride);
+	else lattice_octave_run_t<GRAD, VALUE, false>(rc, R, f, amp, key, acc, stride);
 }
 
 // cellular noise (one octave) over samples [r0, r0 + CELL_SUB); DIST/OP fixed
@@ -212,6 +227,7 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 // kept with integer min/max, and the winners' exact distances and difference
 // vectors are rebuilt from the ids.
 UP_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
+template<bool B> struct BoolTag { static constexpr bool value = B; };
 UP_HD uint32_t umax32(uint32_t a, uint32_t b) { return a > b ? a : b; }
 template<int DIST>
 UP_HD float cell_metric(float vx, float e2yz, float m1yz) {
@@ -273,11 +289,12 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 	int off = 0; // table index of candidate id: id + off
 	int ty = 1, tz = 1; // table cell of this lane's own cell
 	bool table = false;
+	const CellEntry *ct = nullptr; // the warp's shared candidate table (device builds)
 #ifdef __CUDA_ARCH__
 	const int iymin = __reduce_min_sync(0xFFFFFFFFu, iy), iymax = __reduce_max_sync(0xFFFFFFFFu, iy);
 	const int izmin = __reduce_min_sync(0xFFFFFFFFu, iz), izmax = __reduce_max_sync(0xFFFFFFFFu, iz);
 	table = iymax - iymin <= 1 && izmax - izmin <= 1; // the same for every lane
-	const CellEntry *ct = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
+	ct = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
 	if (table) {
 		CellEntry *w = g_runs_cells + (threadIdx.x >> 5) * (CT * CT * CT);
 		__syncwarp(); // the previous sub-run's readers are done
@@ -290,15 +307,18 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 		tz = iz - izmin + 1;
 	}
 #endif
+	const float tyf = (float)ty, tzf = (float)tz;
+	// the candidate search and the winners, compiled once for the shared
+	// table (TABLE) and once for per-lane hashing, so that neither loop
+	// branches per candidate
+	auto search = [&](auto table_tag) {
+	constexpr bool TABLE = decltype(table_tag)::value;
 	// candidate cell with id (column, dy + 1, dz + 1) of this lane
 	auto cand = [&](int id) -> CellEntry {
-#ifdef __CUDA_ARCH__
-		if (table) return ct[id + off];
-#endif
+		if (TABLE) return ct[id + off];
 		return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
 			(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)), id);
 	};
-	const float tyf = (float)ty, tzf = (float)tz;
 	#pragma unroll 1
 	for (int col = 0; col < ncol; col++) {
 		// a column outside a sample's 3x3x3 neighbourhood is pushed far away
@@ -359,11 +379,15 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			case 5: n = a * b * 0.5f - 1.f; dn = (dF1 * b + dF2 * a) * 0.5f; break;
 			default: n = a / b - 1.f; dn = (dF1 * b - dF2 * a) * (1.f / (b * b)); break;
 		}
-		float s = n, ds = 1.f;
-		if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
+		// ridged: s = 1 - 2|n|, selected without a branch
+		const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
+		const float ds = ridged ? (n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f)) : 1.f;
 		const float k = -amp * ds * f;
 		acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
 	}
+	};
+	if (table) search(BoolTag<true>());
+	else search(BoolTag<false>());
 	return true;
 }
 

@@ -84,6 +84,41 @@ struct NG { float v; V3f g; };
 UP_HD NG ng(float v, V3f g) { NG r; r.v = v; r.g = g; return r; }
 UP_HD NG ngc(float v) { return ng(v, zero3()); }
 
+// Pairs of FP32 values for the packed FP32x2 instructions of sm_100+ (one
+// issue slot for two independent FP32 operations, each rounded as its scalar
+// form): fma2(a, b, c) = (fma(a.x, b.x, c.x), fma(a.y, b.y, c.y)), add2 and
+// mul2 likewise. Host builds compute the same correctly rounded results one
+// element at a time.
+struct P2 { float x, y; };
+UP_HD P2 p2(float x, float y) { P2 r; r.x = x; r.y = y; return r; }
+UP_HD P2 p2s(float s) { return p2(s, s); }
+UP_HD P2 fma2(P2 a, P2 b, P2 c) {
+#ifdef __CUDA_ARCH__
+	const float2 r = __ffma2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y), make_float2(c.x, c.y));
+	return p2(r.x, r.y);
+#else
+	return p2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+UP_HD P2 add2(P2 a, P2 b) {
+#ifdef __CUDA_ARCH__
+	const float2 r = __fadd2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+	return p2(r.x, r.y);
+#else
+	volatile float x = a.x + b.x, y = a.y + b.y;
+	return p2(x, y);
+#endif
+}
+UP_HD P2 mul2(P2 a, P2 b) {
+#ifdef __CUDA_ARCH__
+	const float2 r = __fmul2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+	return p2(r.x, r.y);
+#else
+	volatile float x = a.x * b.x, y = a.y * b.y;
+	return p2(x, y);
+#endif
+}
+
 UP_HD float saturatef(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
 UP_HD float lerpf(float a, float b, float t) { return a + (b - a) * t; }
 

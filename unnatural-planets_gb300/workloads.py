@@ -130,6 +130,14 @@ def shell_points(P_radius: float, thickness: float, n: int, seed: int) -> np.nda
 # FMA counts 2; besides these, 8 divisions, 37 square roots and 21 floors per
 # sample are counted apart and not included). Checked by tests/test_oracle.py.
 FLOPS_PER_SAMPLE_C2 = 960.8
+# The same program's value together with its gradient dd/dp, counted with the
+# oracle's sparse forward-mode scalar over the same samples (each operation on
+# a quantity that depends on p also updates its three derivative lanes):
+# 4434.4 FP32 operations per sample (53 divisions, 37 square roots, 21 floors
+# besides). Forward mode is an upper bound on the gradient's work: the GPU
+# kernel's closed-form derivatives (per-face coefficients, the cellular
+# winners' difference vectors) need far fewer. Checked by tests/test_oracle.py.
+FLOPS_PER_SAMPLE_C2_FWD_GRAD = 4434.4
 
 
 def quad_atlas(pos: np.ndarray, nrm: np.ndarray, idx: np.ndarray, width: int, height: int):
