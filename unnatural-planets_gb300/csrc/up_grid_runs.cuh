@@ -134,14 +134,28 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 	const uint32_t y0 = (uint32_t)iy * HY, z0 = ((uint32_t)iz * HZ) ^ key, z1 = ((uint32_t)iz * HZ + HZ) ^ key;
 	const uint32_t yz[4] = {y0 ^ z0, (y0 + HY) ^ z0, y0 ^ z1, (y0 + HY) ^ z1};
 	const float ys[4] = {fy, fy - 1.f, fy, fy - 1.f}, zs[4] = {fz, fz, fz - 1.f, fz - 1.f};
+	// starts: bit r set when sample r begins a segment (its x cell differs
+	// from sample r - 1's), the same for every lane
 #ifdef __CUDA_ARCH__
 	XTab *tab = g_runs_xtab + (threadIdx.x >> 5) * RUN_R;
 	__syncwarp(); // every lane has finished reading the previous octave's table
-	if ((int)(threadIdx.x & 31) < R) tab[threadIdx.x & 31] = xtab_entry(rc, (int)(threadIdx.x & 31), f);
+	const int lane = (int)(threadIdx.x & 31);
+	int mycx = 0;
+	if (lane < R) {
+		const XTab e = xtab_entry(rc, lane, f);
+		tab[lane] = e;
+		mycx = e.cx;
+	}
+	const int leftcx = __shfl_up_sync(0xFFFFFFFFu, mycx, 1);
+	const uint32_t starts = __ballot_sync(0xFFFFFFFFu, lane < R && (lane == 0 || mycx != leftcx));
 	__syncwarp();
 #else
 	XTab tab[RUN_R];
-	for (int q = 0; q < R; q++) tab[q] = xtab_entry(rc, q, f);
+	uint32_t starts = 0;
+	for (int q = 0; q < R; q++) {
+		tab[q] = xtab_entry(rc, q, f);
+		if (q == 0 || tab[q].cx != tab[q - 1].cx) starts |= 1u << q;
+	}
 #endif
 	// coefficients of the two x faces of the current cell; when the next
 	// segment is the neighbouring cell, its low face is the old high face
@@ -151,6 +165,9 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 	#pragma unroll 1
 	while (r < R) { // one segment of samples sharing an x cell (the same for every lane)
 		const int cx = tab[r].cx;
+		// the segment's end: the next start after r, or R
+		const uint32_t later = starts & ~((2u << r) - 1u);
+		const int r1 = later ? lowest_bit(later) : R;
 		const bool carry = r > 0 && cx == cx_prev + 1;
 		cx_prev = cx;
 		if (carry) { GX[0] = GX[1]; Cc[0] = Cc[1]; Py[0] = Py[1]; Qy[0] = Qy[1]; Pz[0] = Pz[1]; Qz[0] = Qz[1]; }
@@ -188,9 +205,8 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 			GX[h] = gc.x; Cc[h] = gc.y; Py[h] = pyz.x; Qy[h] = qyz.x; Pz[h] = pyz.y; Qz[h] = qyz.y;
 		}
 		#pragma unroll 1
-		for (; r < R; r++) {
+		for (; r < r1; r++) {
 			const XTab e = tab[r];
-			if (e.cx != cx) break;
 			const float fx = e.fx;
 			const float u = e.u;
 			const float A0 = VALUE ? Cc[0] : fx * GX[0] + Cc[0];
@@ -228,6 +244,7 @@ UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool 
 // vectors are rebuilt from the ids.
 UP_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
 template<bool B> struct BoolTag { static constexpr bool value = B; };
+template<int I> struct IntTag { static constexpr int value = I; };
 UP_HD uint32_t umax32(uint32_t a, uint32_t b) { return a > b ? a : b; }
 template<int DIST>
 UP_HD float cell_metric(float vx, float e2yz, float m1yz) {
@@ -319,6 +336,56 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 		return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
 			(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)), id);
 	};
+	// Value-only evaluation of an operation on the two distances (not on the
+	// nearest cell's hash): the two smallest metric values themselves are
+	// kept (FP32 min/max, no candidate ids), so no winner is rebuilt. The
+	// keyed search below ranks candidates whose distances agree to 2^-17
+	// relative by id instead; only such near-ties can differ between the two.
+	constexpr bool EXACT = !GRAD && OP != 0;
+	if (EXACT) {
+		float F1[S], F2[S];
+		#pragma unroll
+		for (int r = 0; r < S; r++) { F1[r] = INFINITY; F2[r] = INFINITY; }
+		#pragma unroll 1
+		for (int col = 0; col < ncol; col++) {
+			float sc[S];
+			#pragma unroll
+			for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
+			#pragma unroll 1
+			for (int dy = -1; dy <= 1; dy++) {
+				#pragma unroll
+				for (int dz = -1; dz <= 1; dz++) {
+					const CellEntry ce = cand(col * 16 + (dy + 1) * 4 + (dz + 1));
+					const float vy = (ce.jy - tyf) - fy;
+					const float vz = (ce.jz - tzf) - fz;
+					const float T = ce.jx;
+					const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
+					#pragma unroll
+					for (int r = 0; r < S; r++) {
+						const float m = cell_metric<DIST>(T - sc[r], e2yz, m1yz);
+						F2[r] = fminf(F2[r], fmaxf(F1[r], m));
+						F1[r] = fminf(F1[r], m);
+					}
+				}
+			}
+		}
+		#pragma unroll 1
+		for (int r = 0; r < S; r++) {
+			const float a = DIST == 0 ? sqrtf(F1[r]) : F1[r], b = DIST == 0 ? sqrtf(F2[r]) : F2[r];
+			float n;
+			switch (OP) {
+				case 1: n = a - 1.f; break;
+				case 2: n = b - 1.f; break;
+				case 3: n = (a + b) * 0.5f - 1.f; break;
+				case 4: n = b - a - 1.f; break;
+				case 5: n = a * b * 0.5f - 1.f; break;
+				default: n = a / b - 1.f; break;
+			}
+			const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
+			acc_add(acc, (r0 + r) * stride, -amp * s, 0.f, 0.f, 0.f);
+		}
+		return;
+	}
 	#pragma unroll 1
 	for (int col = 0; col < ncol; col++) {
 		// a column outside a sample's 3x3x3 neighbourhood is pushed far away
@@ -556,11 +623,21 @@ UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typenam
 			filled = true;
 		}
 	}
-	#pragma unroll 1
-	for (int r = 0; r < R && !filled; r++) {
-		const NG b = synth_base<GRAD>(P, v3(rc.px(r), rc.py, rc.pz), spheres);
-		acc_set(acc, r * stride, b.v, b.g.x, b.g.y, b.g.z);
-		far = far && fabsf(b.v) > band;
+	// the base at every sample, the shape's switch taken once per run
+	auto base_loop = [&](auto base_tag) {
+		constexpr int B = decltype(base_tag)::value;
+		#pragma unroll 1
+		for (int r = 0; r < R && !filled; r++) {
+			const NG b = synth_base<GRAD, B>(P, v3(rc.px(r), rc.py, rc.pz), spheres);
+			acc_set(acc, r * stride, b.v, b.g.x, b.g.y, b.g.z);
+			far = far && fabsf(b.v) > band;
+		}
+	};
+	switch (P.base) {
+		case UP_BASE_SPHERE: base_loop(IntTag<UP_BASE_SPHERE>()); break;
+		case UP_BASE_TORUS: base_loop(IntTag<UP_BASE_TORUS>()); break;
+		case UP_BASE_ROUNDED_BOX: base_loop(IntTag<UP_BASE_ROUNDED_BOX>()); break;
+		default: base_loop(IntTag<UP_BASE_TORUS_SPHERES>()); break;
 	}
 #ifdef __CUDA_ARCH__
 	far = __all_sync(0xFFFFFFFFu, far); // every lane of the warp runs every task

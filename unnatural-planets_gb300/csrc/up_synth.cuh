@@ -114,10 +114,12 @@ UP_HD int lowest_bit(uint32_t m) {
 
 // spheres: bit s clear = sphere s is known to be skipped at p (the test
 // below would skip it; synth_segment_spheres); the others are tested
-template<bool GRAD>
+// BASE >= 0: the base shape fixed at compile time (no per-sample switch);
+// BASE < 0: dispatched on P.base at run time
+template<bool GRAD, int BASE = -1>
 UP_HD NG synth_base(const up_synth_program &P, V3f p, uint32_t spheres = 0xFFFFFFFFu) {
-	switch (P.base) {
-		case UP_BASE_SPHERE: return sphere_d(p, zero3(), P.param[0]);
+	const int base = BASE >= 0 ? BASE : P.base;
+	switch (base) {		case UP_BASE_SPHERE: return sphere_d(p, zero3(), P.param[0]);
 		case UP_BASE_TORUS: return torus_d(p, P.param[0], P.param[1]);
 		case UP_BASE_ROUNDED_BOX: return box_d(p, P.param[0], P.param[1]);
 		default: {
