@@ -52,6 +52,12 @@ CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
 # capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (244.77 MB / 16,777,216)
 TRAFFIC_PER_SAMPLE_FUSED = 244.771584e6 / 16777216
+# FP32 operations executed per sample by the fused grid kernel (FFMA x 2,
+# FFMA2 x 4, FADD, FADD2 x 2, FMUL, FMUL2 x 2 per thread instruction), and its
+# thread instructions per sample, from the ncu instruction counts of
+# synth_grid_runs_kernel<1,2,1301> at 256^3
+EXEC_FP32_PER_SAMPLE_FUSED = 0.0
+INSTR_PER_SAMPLE_FUSED = 0.0
 
 
 def workload_config(grid: int, n: int) -> dict:
@@ -659,9 +665,22 @@ def run_ours(args) -> None:
                                        f"({TRAFFIC_PER_SAMPLE_FUSED:.2f} B/sample), scaled by samples to this launch",
                      "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x {max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)",
                      "flops_per_sample": W.FLOPS_PER_SAMPLE_C2,
-                     "note": "value-path FLOPs of the oracle count; the gradient's extra arithmetic and all integer hashing are not counted; "
-                             "the kernel is issue-bound on the ALU pipe (hashing), see profiles/",
-                     "hbm_view": {"algorithmic_bytes": 16 * N, "achieved_gbs": 16 * N / (t_fused * 1e-3) / 1e9,
+                     "flops_definition": "value path, counted by the oracle's operation-counting FP32 scalar (FMA = 2)",
+                     "value_gradient_fwd_mode": {
+                         "flops_per_sample": W.FLOPS_PER_SAMPLE_C2_FWD_GRAD,
+                         "achieved": W.FLOPS_PER_SAMPLE_C2_FWD_GRAD * N / (t_fused * 1e-3) / 1e12,
+                         "frac": W.FLOPS_PER_SAMPLE_C2_FWD_GRAD * N / (t_fused * 1e-3) / 1e12 / fp32_peak,
+                         "note": "value with dd/dp counted in sparse forward mode by the oracle: an upper bound on the gradient's "
+                                 "arithmetic; the kernel's closed-form derivatives need far fewer operations, so this fraction "
+                                 "overstates how busy the FP32 pipe is (exec_fp32 below is what it executes)"},
+                     "exec_fp32": {"flops_per_sample": EXEC_FP32_PER_SAMPLE_FUSED,
+                                   "achieved": EXEC_FP32_PER_SAMPLE_FUSED * N / (t_fused * 1e-3) / 1e12,
+                                   "frac": EXEC_FP32_PER_SAMPLE_FUSED * N / (t_fused * 1e-3) / 1e12 / fp32_peak,
+                                   "source": "FP32 operations the fused kernel executes per sample (FFMA and FFMA2 lanes x 2, FADD, "
+                                             "FMUL), from the ncu instruction counts at 256^3 (profiles/)"},
+                     "note": "the kernel is instruction-issue bound (about 80 % issue active): per sample it issues about "
+                             f"{INSTR_PER_SAMPLE_FUSED:.0f} thread instructions, of which the cellular candidate keys (integer "
+                             "min/max, bit masks) and control flow are a large share; see profiles/",                     "hbm_view": {"algorithmic_bytes": 16 * N, "achieved_gbs": 16 * N / (t_fused * 1e-3) / 1e9,
                                   "peak_gbs": peaks.get("hbm_gbs"), "frac": (16 * N / (t_fused * 1e-3) / 1e9) / peaks["hbm_gbs"]
                                   if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}},
         "cpu_baseline": {"value": cpu_grad / 1e9, "unit": UNIT, "cores": threads, "kind": "port",

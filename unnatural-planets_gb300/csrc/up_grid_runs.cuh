@@ -329,25 +329,16 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 	// table (TABLE) and once for per-lane hashing, so that neither loop
 	// branches per candidate
 	auto search = [&](auto table_tag) {
-	constexpr bool TABLE = decltype(table_tag)::value;
-	// candidate cell with id (column, dy + 1, dz + 1) of this lane
-	auto cand = [&](int id) -> CellEntry {
-		if (TABLE) return ct[id + off];
-		return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
-			(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)), id);
-	};
-	// Value-only evaluation of an operation on the two distances (not on the
-	// nearest cell's hash): the two smallest metric values themselves are
-	// kept (FP32 min/max, no candidate ids), so no winner is rebuilt. The
-	// keyed search below ranks candidates whose distances agree to 2^-17
-	// relative by id instead; only such near-ties can differ between the two.
-	constexpr bool EXACT = !GRAD && OP != 0;
-	if (EXACT) {
-		float F1[S], F2[S];
-		#pragma unroll
-		for (int r = 0; r < S; r++) { F1[r] = INFINITY; F2[r] = INFINITY; }
+		constexpr bool TABLE = decltype(table_tag)::value;
+		// candidate cell with id (column, dy + 1, dz + 1) of this lane
+		auto cand = [&](int id) -> CellEntry {
+			if (TABLE) return ct[id + off];
+			return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
+				(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)), id);
+		};
 		#pragma unroll 1
 		for (int col = 0; col < ncol; col++) {
+			// a column outside a sample's 3x3x3 neighbourhood is pushed far away
 			float sc[S];
 			#pragma unroll
 			for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
@@ -355,103 +346,62 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			for (int dy = -1; dy <= 1; dy++) {
 				#pragma unroll
 				for (int dz = -1; dz <= 1; dz++) {
-					const CellEntry ce = cand(col * 16 + (dy + 1) * 4 + (dz + 1));
+					const uint32_t id = (uint32_t)(col * 16 + (dy + 1) * 4 + (dz + 1));
+					const CellEntry ce = cand((int)id);
 					const float vy = (ce.jy - tyf) - fy;
 					const float vz = (ce.jz - tzf) - fz;
 					const float T = ce.jx;
 					const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
 					#pragma unroll
 					for (int r = 0; r < S; r++) {
-						const float m = cell_metric<DIST>(T - sc[r], e2yz, m1yz);
-						F2[r] = fminf(F2[r], fmaxf(F1[r], m));
-						F1[r] = fminf(F1[r], m);
+						const uint32_t k = (f_bits(cell_metric<DIST>(T - sc[r], e2yz, m1yz)) & ~63u) | id;
+						K2[r] = umin32(K2[r], umax32(K1[r], k));
+						K1[r] = umin32(K1[r], k);
 					}
 				}
 			}
 		}
 		#pragma unroll 1
 		for (int r = 0; r < S; r++) {
-			const float a = DIST == 0 ? sqrtf(F1[r]) : F1[r], b = DIST == 0 ? sqrtf(F2[r]) : F2[r];
-			float n;
-			switch (OP) {
-				case 1: n = a - 1.f; break;
-				case 2: n = b - 1.f; break;
-				case 3: n = (a + b) * 0.5f - 1.f; break;
-				case 4: n = b - a - 1.f; break;
-				case 5: n = a * b * 0.5f - 1.f; break;
-				default: n = a / b - 1.f; break;
-			}
-			const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
-			acc_add(acc, (r0 + r) * stride, -amp * s, 0.f, 0.f, 0.f);
-		}
-		return;
-	}
-	#pragma unroll 1
-	for (int col = 0; col < ncol; col++) {
-		// a column outside a sample's 3x3x3 neighbourhood is pushed far away
-		float sc[S];
-		#pragma unroll
-		for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
-		#pragma unroll 1
-		for (int dy = -1; dy <= 1; dy++) {
+			float Fw[2];
+			V3f vw[2], dFw[2] = {zero3(), zero3()};
+			uint32_t h1 = 0;
 			#pragma unroll
-			for (int dz = -1; dz <= 1; dz++) {
-				const uint32_t id = (uint32_t)(col * 16 + (dy + 1) * 4 + (dz + 1));
-				const CellEntry ce = cand((int)id);
+			for (int wsel = 0; wsel < 2; wsel++) {
+				const int id = (int)((wsel ? K2[r] : K1[r]) & 63u);
+				const CellEntry ce = cand(id);
 				const float vy = (ce.jy - tyf) - fy;
 				const float vz = (ce.jz - tzf) - fz;
-				const float T = ce.jx;
-				const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
-				#pragma unroll
-				for (int r = 0; r < S; r++) {
-					const uint32_t k = (f_bits(cell_metric<DIST>(T - sc[r], e2yz, m1yz)) & ~63u) | id;
-					K2[r] = umin32(K2[r], umax32(K1[r], k));
-					K1[r] = umin32(K1[r], k);
+				const float vx = ce.jx - sx[r];
+				const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
+				Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
+				vw[wsel] = v3(vx, vy, vz);
+				if (GRAD) {
+					// d F / d p for v = q - p (dv/dp = -I); Euclidean: -v / |v|
+					if (DIST == 0) dFw[wsel] = d > 0.f ? vw[wsel] * -rsqrt_hd(d) : zero3();
+					else dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
 				}
+				if (!wsel) h1 = ce.h;
 			}
-		}
-	}
-	#pragma unroll 1
-	for (int r = 0; r < S; r++) {
-		float Fw[2];
-		V3f vw[2], dFw[2] = {zero3(), zero3()};
-		uint32_t h1 = 0;
-		#pragma unroll
-		for (int wsel = 0; wsel < 2; wsel++) {
-			const int id = (int)((wsel ? K2[r] : K1[r]) & 63u);
-			const CellEntry ce = cand(id);
-			const float vy = (ce.jy - tyf) - fy;
-			const float vz = (ce.jz - tzf) - fz;
-			const float vx = ce.jx - sx[r];
-			const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
-			Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
-			vw[wsel] = v3(vx, vy, vz);
-			if (GRAD) {
-				// d F / d p for v = q - p (dv/dp = -I); Euclidean: -v / |v|
-				if (DIST == 0) dFw[wsel] = d > 0.f ? vw[wsel] * -rsqrt_hd(d) : zero3();
-				else dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
+			const float a = Fw[0], b = Fw[1];
+			const V3f dF1 = dFw[0], dF2 = dFw[1];
+			float n;
+			V3f dn;
+			switch (OP) {
+				case 0: n = hash_signed(mix32(h1)); dn = zero3(); break;
+				case 1: n = a - 1.f; dn = dF1; break;
+				case 2: n = b - 1.f; dn = dF2; break;
+				case 3: n = (a + b) * 0.5f - 1.f; dn = (dF1 + dF2) * 0.5f; break;
+				case 4: n = b - a - 1.f; dn = dF2 - dF1; break;
+				case 5: n = a * b * 0.5f - 1.f; dn = (dF1 * b + dF2 * a) * 0.5f; break;
+				default: n = a / b - 1.f; dn = (dF1 * b - dF2 * a) * (1.f / (b * b)); break;
 			}
-			if (!wsel) h1 = ce.h;
+			// ridged: s = 1 - 2|n|, selected without a branch
+			const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
+			const float ds = ridged ? (n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f)) : 1.f;
+			const float k = -amp * ds * f;
+			acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
 		}
-		const float a = Fw[0], b = Fw[1];
-		const V3f dF1 = dFw[0], dF2 = dFw[1];
-		float n;
-		V3f dn;
-		switch (OP) {
-			case 0: n = hash_signed(mix32(h1)); dn = zero3(); break;
-			case 1: n = a - 1.f; dn = dF1; break;
-			case 2: n = b - 1.f; dn = dF2; break;
-			case 3: n = (a + b) * 0.5f - 1.f; dn = (dF1 + dF2) * 0.5f; break;
-			case 4: n = b - a - 1.f; dn = dF2 - dF1; break;
-			case 5: n = a * b * 0.5f - 1.f; dn = (dF1 * b + dF2 * a) * 0.5f; break;
-			default: n = a / b - 1.f; dn = (dF1 * b - dF2 * a) * (1.f / (b * b)); break;
-		}
-		// ridged: s = 1 - 2|n|, selected without a branch
-		const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
-		const float ds = ridged ? (n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f)) : 1.f;
-		const float k = -amp * ds * f;
-		acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
-	}
 	};
 	if (table) search(BoolTag<true>());
 	else search(BoolTag<false>());
