@@ -118,9 +118,13 @@ UP_HD void acc_add_fma(float *acc, int i, float a, float b, float, float, float)
 
 // one octave of lattice noise (VALUE = value noise, else Perlin); subtracts
 // amp * s(n) (s = n or 1 - 2|n|) from every sample of the run
-// RIDGED is a compile-time flag: the per-sample loop carries no branch on it
-template<bool GRAD, bool VALUE, bool RIDGED>
-UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
+// RIDGED: 1 ridged, 0 not, both fixed at compile time (the per-sample loop
+// carries no branch on it); -1 taken from ridged_rt at run time (one
+// instantiation for callers that hold many noise instances in one kernel)
+template<bool GRAD, bool VALUE, int RIDGED>
+UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uint32_t key, typename AccOf<GRAD>::T *acc, int stride,
+	bool ridged_rt = false) {
+	const bool ridged = RIDGED < 0 ? ridged_rt : RIDGED == 1;
 	const float qy = rc.py * f, qz = rc.pz * f;
 	const float fy0 = floorf(qy), fz0 = floorf(qz);
 	const int iy = (int)fy0, iz = (int)fz0;
@@ -214,7 +218,7 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 			const float dA = A1 - A0;
 			const float n = A0 + u * dA;
 			float s = n, ds = 1.f;
-			if (RIDGED) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
+			if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
 			if (GRAD) {
 				const float du = e.du;
 				const float dnx = (VALUE ? 0.f : GX[0] + u * (GX[1] - GX[0])) + du * dA;
@@ -230,8 +234,8 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 }
 template<bool GRAD, bool VALUE>
 UP_HD void lattice_octave_run(const RunCtx &rc, int R, float f, float amp, bool ridged, uint32_t key, typename AccOf<GRAD>::T *acc, int stride) {
-	if (ridged) lattice_octave_run_t<GRAD, VALUE, true>(rc, R, f, amp, key, acc, stride);
-	else lattice_octave_run_t<GRAD, VALUE, false>(rc, R, f, amp, key, acc, stride);
+	if (ridged) lattice_octave_run_t<GRAD, VALUE, 1>(rc, R, f, amp, key, acc, stride);
+	else lattice_octave_run_t<GRAD, VALUE, 0>(rc, R, f, amp, key, acc, stride);
 }
 
 // cellular noise (one octave) over samples [r0, r0 + CELL_SUB); DIST/OP fixed

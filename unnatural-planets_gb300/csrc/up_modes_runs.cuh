@@ -63,8 +63,10 @@ template<int EM> UP_HD void modes_run_fill(const ModesDesc &M, const RunCtx &rc,
 		for (int i = 0; i < n.octaves; i++) {
 			const uint32_t key = seed_key(n.seed + (uint32_t)i);
 			const bool ridged = n.fractal == UP_FRACTAL_RIDGED;
-			if (n.type == UP_NOISE_VALUE) lattice_octave_run<false, true>(rc, R, n.freq[i], -n.amp[i], ridged, key, slot, stride);
-			else lattice_octave_run<false, false>(rc, R, n.freq[i], -n.amp[i], ridged, key, slot, stride);
+			// the ridged flag at run time: one instantiation per noise type keeps
+			// this kernel's code small
+			if (n.type == UP_NOISE_VALUE) lattice_octave_run_t<false, true, -1>(rc, R, n.freq[i], -n.amp[i], key, slot, stride, ridged);
+			else lattice_octave_run_t<false, false, -1>(rc, R, n.freq[i], -n.amp[i], key, slot, stride, ridged);
 		}
 	}
 }
