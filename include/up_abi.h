@@ -199,6 +199,12 @@ size_t up_context_device_bytes(const up_context *ctx);
  * allocations of any context fail as if the device were out of memory
  * (the call returns UP_ERR_OOM). No reference counterpart. */
 void up_debug_fail_allocations(uint32_t count);
+/* Wait limit, in nanoseconds of the GPU's global timer, of every grid-wide
+ * barrier of the persistent batch launch (up_batch_run); 0 restores the
+ * default of 2 s. A wait that runs out makes the call return UP_ERR_TIMEOUT
+ * and leaves the launch without blocking. For tests of that path; no
+ * reference counterpart. */
+void up_debug_set_wait_limit(uint64_t ns);
 /* Seed of noise instance slot i for planet seed s (math.cpp:73-77 replaced). */
 uint32_t up_instance_seed(uint32_t seed, uint32_t slot);
 
@@ -346,10 +352,15 @@ typedef struct up_batch_out {
 	float *values;        /* optional: the sampled grids of all chunks, concatenated (x-fastest per chunk) */
 	uint64_t values_capacity;
 } up_batch_out;
-/* Samples and contours many chunks of uneven size (from many planets) in one
- * pass per stage, each stage one launch over all chunks, replayed as a CUDA
- * graph when the same chunk list is run again. The closest reference
- * counterpart is the per-chunk tasksRunBlocking fan-out (generator.cpp:159,215).
+/* Samples and contours many chunks of uneven size (from many planets). The
+ * first call for a chunk list runs one launch per stage over all chunks (the
+ * host sizes the lists from the counts), autotunes the sampling tile shape,
+ * and captures a CUDA graph for later calls with the same list: one
+ * persistent, cooperatively launched kernel that runs every stage as a phase
+ * separated by grid-wide barriers (bounded waits: UP_ERR_TIMEOUT when one runs
+ * out), or the stage launches where a cooperative launch is not available.
+ * The closest reference counterpart is the per-chunk tasksRunBlocking fan-out
+ * (generator.cpp:159,215).
  * Indices of chunk c are local to chunk c's vertices. Without a values buffer
  * the chunks are sampled with the narrow band of contouring (see up_contour;
  * the meshes are the same); with one, every sample is exact. */

@@ -83,3 +83,27 @@ def test_batch_narrow_band_equals_exact(cuda, up):
     banded = up.batch_run(ctx, planets, chunks, values=False)
     for k in ("positions", "indices", "vertex_offsets", "index_offsets"):
         assert np.array_equal(exact[k], banded[k]), k
+
+
+def test_batch_persistent_wait_runs_out(cuda, up):
+    """Replays run the batch as one persistent cooperative launch whose
+    phases meet at grid-wide barriers with bounded waits. With a wait limit
+    of 1 ns the waits run out: the call returns UP_ERR_TIMEOUT and the launch
+    ends (no block keeps waiting). With the default limit restored the next
+    replay reproduces the first run."""
+    W = workloads()
+    planets, chunks = W.chunk_set(n_planets=4, n_chunks=16, seed=6, edge_lo=16, edge_hi=40)
+    ctx = up.Planet(program=planets[0])
+    res = up.batch_run(ctx, planets, chunks, values=True)
+    first = {k: np.copy(res[k]) for k in ("positions", "indices", "values")}
+    try:
+        ctx.lib.up_debug_set_wait_limit(1)
+        with pytest.raises(up.UpError) as e:
+            up.batch_replay(ctx, res)
+        assert e.value.status == up.abi.UP_ERR_TIMEOUT
+        assert b"barrier" in ctx.lib.up_last_error(ctx.h)
+    finally:
+        ctx.lib.up_debug_set_wait_limit(0)
+    up.batch_replay(ctx, res)
+    for k in first:
+        assert np.array_equal(res[k], first[k]), k

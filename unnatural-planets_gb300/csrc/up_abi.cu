@@ -34,7 +34,8 @@ cudaError_t tiles_run(const ModesDesc *M, int purpose, const float *pos, const f
 void batch_state_free(void *p);
 cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t nplanets, const up_chunk *chunks, size_t nchunks,
 	bool exact_values, uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
-	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, cudaStream_t caller);
+	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, unsigned &fault, cudaStream_t caller);
+void batch_set_wait_limit(unsigned long long ns);
 } // namespace up
 
 using namespace up;
@@ -506,6 +507,8 @@ size_t up_context_device_bytes(const up_context *ctx) {
 
 void up_debug_fail_allocations(uint32_t count) { g_fail_allocs.store(count); }
 
+void up_debug_set_wait_limit(uint64_t ns) { batch_set_wait_limit(ns); }
+
 int up_context_set_stream(up_context *ctx, void *stream) {
 	if (!ctx) return UP_ERR_INVALID_ARGUMENT;
 	ctx->stream = (cudaStream_t)stream;
@@ -908,8 +911,11 @@ int up_batch_run(up_context *ctx, const up_synth_program *planets, size_t nplane
 		const uint32_t *didx = nullptr;
 		uint64_t nval = 0;
 		bool nan = false, replayed = false;
+		unsigned fault = 0;
 		check(batch_execute(ctx->batch, planets, nplanets, chunks, nchunks, out->values != nullptr, ncells, nquads, cc, cq, dpos, didx, dval, nval,
-			nan, replayed, ctx->stream), "batch kernels");
+			nan, replayed, fault, ctx->stream), "batch kernels");
+		if (fault & 1u) return fail(ctx, UP_ERR_TIMEOUT, "batch: a grid barrier wait of the persistent launch ran out; the outputs are not valid");
+		if (fault) return fail(ctx, UP_ERR_CUDA, "batch: the persistent launch's counts differ from the plan; the outputs are not valid");
 		if (nan) return fail(ctx, UP_ERR_NAN, "invalid land sdf value");
 		out->vertex_count = ncells;
 		out->index_count = 6ull * nquads;
