@@ -50,14 +50,14 @@ METRIC = "SDF+grad Gsamples/s at 512^3 (fused value+gradient; plain and ms/plane
 UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
-# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (244.77 MB / 16,777,216)
-TRAFFIC_PER_SAMPLE_FUSED = 244.771584e6 / 16777216
+# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (0.256 MB + 244.18 MB
+# over 16,777,216 samples)
+TRAFFIC_PER_SAMPLE_FUSED = 244.438528e6 / 16777216
 # FP32 operations executed per sample by the fused grid kernel (FFMA x 2,
-# FFMA2 x 4, FADD, FADD2 x 2, FMUL, FMUL2 x 2 per thread instruction), and its
-# thread instructions per sample, from the ncu instruction counts of
-# synth_grid_runs_kernel<1,2,1301> at 256^3
-EXEC_FP32_PER_SAMPLE_FUSED = 0.0
-INSTR_PER_SAMPLE_FUSED = 0.0
+# FFMA2 x 4, FADD, FMUL per thread instruction) and its thread instructions per
+# sample, from the ncu instruction counts of the same capture
+EXEC_FP32_PER_SAMPLE_FUSED = 754.9
+INSTR_PER_SAMPLE_FUSED = 1162.4
 
 
 def workload_config(grid: int, n: int) -> dict:

@@ -205,6 +205,12 @@ void up_debug_fail_allocations(uint32_t count);
  * and leaves the launch without blocking. For tests of that path; no
  * reference counterpart. */
 void up_debug_set_wait_limit(uint64_t ns);
+/* Which form up_batch_run replays for chunk lists planned after this call:
+ * 0 (default) the faster of the two, timed on the list when it is planned;
+ * 1 the stage launches; 2 the persistent launch (where the device supports
+ * cooperative launches). For tests and measurements; no reference
+ * counterpart. Returns UP_ERR_INVALID_ARGUMENT for another value. */
+int up_debug_set_batch_form(int form);
 /* Seed of noise instance slot i for planet seed s (math.cpp:73-77 replaced). */
 uint32_t up_instance_seed(uint32_t seed, uint32_t slot);
 
@@ -355,10 +361,11 @@ typedef struct up_batch_out {
 /* Samples and contours many chunks of uneven size (from many planets). The
  * first call for a chunk list runs one launch per stage over all chunks (the
  * host sizes the lists from the counts), autotunes the sampling tile shape,
- * and captures a CUDA graph for later calls with the same list: one
+ * and captures a CUDA graph for later calls with the same list: either one
  * persistent, cooperatively launched kernel that runs every stage as a phase
  * separated by grid-wide barriers (bounded waits: UP_ERR_TIMEOUT when one runs
- * out), or the stage launches where a cooperative launch is not available.
+ * out), or the stage launches, whichever ran faster on the list when it was
+ * planned (up_debug_set_batch_form fixes the choice).
  * The closest reference counterpart is the per-chunk tasksRunBlocking fan-out
  * (generator.cpp:159,215).
  * Indices of chunk c are local to chunk c's vertices. Without a values buffer

@@ -86,7 +86,7 @@ def test_batch_narrow_band_equals_exact(cuda, up):
 
 
 def test_batch_persistent_wait_runs_out(cuda, up):
-    """Replays run the batch as one persistent cooperative launch whose
+    """The persistent form replays the batch as one cooperative launch whose
     phases meet at grid-wide barriers with bounded waits. With a wait limit
     of 1 ns the waits run out: the call returns UP_ERR_TIMEOUT and the launch
     ends (no block keeps waiting). With the default limit restored the next
@@ -94,7 +94,11 @@ def test_batch_persistent_wait_runs_out(cuda, up):
     W = workloads()
     planets, chunks = W.chunk_set(n_planets=4, n_chunks=16, seed=6, edge_lo=16, edge_hi=40)
     ctx = up.Planet(program=planets[0])
-    res = up.batch_run(ctx, planets, chunks, values=True)
+    assert ctx.lib.up_debug_set_batch_form(2) == 0   # plan the persistent form whatever its speed
+    try:
+        res = up.batch_run(ctx, planets, chunks, values=True)
+    finally:
+        ctx.lib.up_debug_set_batch_form(0)
     first = {k: np.copy(res[k]) for k in ("positions", "indices", "values")}
     try:
         ctx.lib.up_debug_set_wait_limit(1)
@@ -107,3 +111,33 @@ def test_batch_persistent_wait_runs_out(cuda, up):
     up.batch_replay(ctx, res)
     for k in first:
         assert np.array_equal(res[k], first[k]), k
+
+
+@pytest.mark.parametrize("form", [1, 2])
+def test_batch_forms_equal_per_chunk(cuda, up, form):
+    """Both replayed forms (the stage launches, the persistent launch) give
+    the meshes of one up_contour call per chunk, bit for bit."""
+    import ctypes as C
+    W = workloads()
+    planets, chunks = W.chunk_set(n_planets=5, n_chunks=20, seed=8, edge_lo=12, edge_hi=36)
+    ctx = up.Planet(program=planets[0])
+    assert ctx.lib.up_debug_set_batch_form(form) == 0
+    try:
+        res = up.batch_run(ctx, planets, chunks, values=True)
+        up.batch_replay(ctx, res)
+    finally:
+        ctx.lib.up_debug_set_batch_form(0)
+    vo, io = res["vertex_offsets"], res["index_offsets"]
+    off = 0
+    for c, (p, g) in enumerate(chunks):
+        n = g.count
+        vals = res["values"][off:off + n]
+        off += n
+        single = up.Planet(program=planets[p])
+        m = up.abi.MeshOut()
+        if single.lib.up_contour(single.h, 0, C.byref(g), vals.ctypes.data, C.byref(m)) == up.abi.UP_ERR_EMPTY_MESH:
+            assert io[c + 1] == io[c]
+            continue
+        pos, _, idx = single.contour(g, values=vals)
+        assert np.array_equal(res["indices"][io[c]:io[c + 1]], idx)
+        assert np.allclose(res["positions"][vo[c]:vo[c + 1]], pos, rtol=0, atol=1e-5)

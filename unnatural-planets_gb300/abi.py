@@ -113,6 +113,7 @@ SIGNATURES = [
     ("up_context_device_bytes", C.c_size_t, [C.c_void_p]),
     ("up_debug_fail_allocations", None, [C.c_uint32]),
     ("up_debug_set_wait_limit", None, [C.c_uint64]),
+    ("up_debug_set_batch_form", C.c_int, [C.c_int]),
     ("up_instance_seed", C.c_uint32, [C.c_uint32, C.c_uint32]),
     ("up_sdf_eval_points", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     ("up_set_current_context", C.c_int, [C.c_void_p]),

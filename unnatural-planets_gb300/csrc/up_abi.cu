@@ -36,6 +36,7 @@ cudaError_t batch_execute(void *&state, const up_synth_program *planets, size_t 
 	bool exact_values, uint32_t &ncells, uint32_t &nquads, std::vector<uint32_t> &chunk_cells, std::vector<uint32_t> &chunk_quads, const float *&dpos,
 	const uint32_t *&didx, const float *&dvalues, uint64_t &nvalues, bool &nan, bool &replayed, unsigned &fault, cudaStream_t caller);
 void batch_set_wait_limit(unsigned long long ns);
+void batch_set_form(int form);
 } // namespace up
 
 using namespace up;
@@ -508,6 +509,12 @@ size_t up_context_device_bytes(const up_context *ctx) {
 void up_debug_fail_allocations(uint32_t count) { g_fail_allocs.store(count); }
 
 void up_debug_set_wait_limit(uint64_t ns) { batch_set_wait_limit(ns); }
+
+int up_debug_set_batch_form(int form) {
+	if (form < 0 || form > 2) return UP_ERR_INVALID_ARGUMENT;
+	batch_set_form(form);
+	return UP_OK;
+}
 
 int up_context_set_stream(up_context *ctx, void *stream) {
 	if (!ctx) return UP_ERR_INVALID_ARGUMENT;
