@@ -307,7 +307,6 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 	#pragma unroll
 	for (int r = 0; r < S; r++) { K1[r] = 0xFFFFFFFFu; K2[r] = 0xFFFFFFFFu; }
 	const int ncol = ixb - ixa + 3;
-	int off = 0; // table index of candidate id: id + off
 	int ty = 1, tz = 1; // table cell of this lane's own cell
 	bool table = false;
 	const CellEntry *ct = nullptr; // the warp's shared candidate table (device builds)
@@ -323,48 +322,124 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			w[e] = cell_entry(mix32(((uint32_t)(ixa - 1 + (e >> 4)) * HX) ^ ((uint32_t)(iymin - 1 + ((e >> 2) & 3)) * HY) ^
 				(((uint32_t)(izmin - 1 + (e & 3)) * HZ) ^ key)), e);
 		__syncwarp();
-		off = (iy - iymin) * CT + (iz - izmin);
 		ty = iy - iymin + 1;
 		tz = iz - izmin + 1;
 	}
 #endif
 	const float tyf = (float)ty, tzf = (float)tz;
+	// candidate (feature point ce, key id) against the sub-run's samples; with
+	// MASKED, samples r outside [rlo, rhi) do not see it (pushed far away)
+	auto visit = [&](auto masked_tag, uint32_t id, const CellEntry &ce, float T, int rlo, int rhi) {
+		constexpr bool MASKED = decltype(masked_tag)::value;
+		const float vy = (ce.jy - tyf) - fy;
+		const float vz = (ce.jz - tzf) - fz;
+		const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
+		#pragma unroll
+		for (int r = 0; r < S; r++) {
+			const float s = MASKED && (r < rlo || r >= rhi) ? -1e18f : sx[r];
+			const uint32_t k = (f_bits(cell_metric<DIST>(T - s, e2yz, m1yz)) & ~63u) | id;
+			K2[r] = umin32(K2[r], umax32(K1[r], k));
+			K1[r] = umin32(K1[r], k);
+		}
+	};
 	// the candidate search and the winners, compiled once for the shared
 	// table (TABLE) and once for per-lane hashing, so that neither loop
 	// branches per candidate
 	auto search = [&](auto table_tag) {
 		constexpr bool TABLE = decltype(table_tag)::value;
-		// candidate cell with id (column, dy + 1, dz + 1) of this lane
+		// TABLE: the candidate of table index id (keys carry table indices:
+		// the lane's own ids plus the per-lane constant (ty - 1) * 4 + (tz - 1),
+		// so the order by key is that of the per-lane search); otherwise the
+		// lane's candidate (column, dy + 1, dz + 1)
 		auto cand = [&](int id) -> CellEntry {
-			if (TABLE) return ct[id + off];
+			if (TABLE) return ct[id];
 			return cell_entry(mix32(((uint32_t)(ixa - 1 + (id >> 4)) * HX) ^ ((uint32_t)(iy - 1 + ((id >> 2) & 3)) * HY) ^
 				(((uint32_t)(iz - 1 + (id & 3)) * HZ) ^ key)), id);
 		};
-		#pragma unroll 1
-		for (int col = 0; col < ncol; col++) {
-			// a column outside a sample's 3x3x3 neighbourhood is pushed far away
-			float sc[S];
-			#pragma unroll
-			for (int r = 0; r < S; r++) sc[r] = ((col == 0 && r >= split) || (col == 3 && r < split)) ? -1e18f : sx[r];
+		if (!TABLE) {
 			#pragma unroll 1
-			for (int dy = -1; dy <= 1; dy++) {
-				#pragma unroll
-				for (int dz = -1; dz <= 1; dz++) {
-					const uint32_t id = (uint32_t)(col * 16 + (dy + 1) * 4 + (dz + 1));
-					const CellEntry ce = cand((int)id);
-					const float vy = (ce.jy - tyf) - fy;
-					const float vz = (ce.jz - tzf) - fz;
-					const float T = ce.jx;
-					const float e2yz = vy * vy + vz * vz, m1yz = fabsf(vy) + fabsf(vz);
+			for (int col = 0; col < ncol; col++) {
+				// a column outside a sample's 3x3x3 neighbourhood: samples of the
+				// other x cell only
+				const int rlo = col == 3 ? split : 0, rhi = col == 0 ? split : S;
+				#pragma unroll 1
+				for (int dy = -1; dy <= 1; dy++) {
 					#pragma unroll
-					for (int r = 0; r < S; r++) {
-						const uint32_t k = (f_bits(cell_metric<DIST>(T - sc[r], e2yz, m1yz)) & ~63u) | id;
-						K2[r] = umin32(K2[r], umax32(K1[r], k));
-						K1[r] = umin32(K1[r], k);
+					for (int dz = -1; dz <= 1; dz++) {
+						const uint32_t id = (uint32_t)(col * 16 + (dy + 1) * 4 + (dz + 1));
+						const CellEntry ce = cand((int)id);
+						visit(BoolTag<true>(), id, ce, ce.jx, rlo, rhi);
 					}
 				}
 			}
 		}
+#ifdef __CUDA_ARCH__
+		if (TABLE) {
+			// Warp-wide pruning. Every sample of the warp lies in the box
+			// [sxmin, sxmax] x [ymin, ymax] x [zmin, zmax] (table coordinates,
+			// a sample's x difference to entry e being jx - sx). Two entries
+			// that every sample sees (its 3 x 3 x 3 neighbourhood, both x
+			// cells) bound F2 by the second smallest of their largest metric
+			// over the box (thr); an entry whose smallest metric over the box
+			// exceeds thr (by 0.1 % + 1e-4, far beyond FP32 rounding and the
+			// keys' 2^-17 quantisation) is outranked by both at every sample,
+			// so it is never one of a sample's two keys and is skipped. The
+			// surviving entries are the same for every lane (no divergence).
+			const uint32_t FULL = 0xFFFFFFFFu;
+			const int lane = (int)(threadIdx.x & 31);
+			float sxmin = sx[0], sxmax = sx[0];
+			#pragma unroll
+			for (int r = 1; r < S; r++) { sxmin = fminf(sxmin, sx[r]); sxmax = fmaxf(sxmax, sx[r]); }
+			// lane positions are positive (ty >= 1): their bits order as the floats
+			const uint32_t ly = f_bits(tyf + fy), lz = f_bits(tzf + fz);
+			const float ymin = bits_f(__reduce_min_sync(FULL, ly)), ymax = bits_f(__reduce_max_sync(FULL, ly));
+			const float zmin = bits_f(__reduce_min_sync(FULL, lz)), zmax = bits_f(__reduce_max_sync(FULL, lz));
+			const int tymax = iymax - iymin + 1, tzmax = izmax - izmin + 1;
+			const int n = ncol * CT * CT, c_lo = ncol == 4 ? 1 : 0;
+			auto bounds = [&](int e, float &lb, float &ub) {
+				const CellEntry c = ct[e];
+				const float ax = sxmin - c.jx, bx = c.jx - sxmax;
+				const float ay = ymin - c.jy, by = c.jy - ymax;
+				const float az = zmin - c.jz, bz = c.jz - zmax;
+				const float nx = fmaxf(fmaxf(ax, bx), 0.f), ny = fmaxf(fmaxf(ay, by), 0.f), nz = fmaxf(fmaxf(az, bz), 0.f);
+				const float fx = fmaxf(-ax, -bx), fy2 = fmaxf(-ay, -by), fz2 = fmaxf(-az, -bz);
+				lb = cell_metric<DIST>(nx, ny * ny + nz * nz, ny + nz);
+				ub = cell_metric<DIST>(fx, fy2 * fy2 + fz2 * fz2, fy2 + fz2);
+			};
+			// seen by every sample: columns of both x cells, y and z inside every lane's window
+			auto everywhere = [&](int e) {
+				const int c = e >> 4, yy = (e >> 2) & 3, zz = e & 3;
+				return c >= c_lo && c <= 2 && yy >= tymax - 1 && yy <= 2 && zz >= tzmax - 1 && zz <= 2;
+			};
+			float lb0, ub0, lb1 = 3e38f, ub1 = 3e38f;
+			const bool has1 = lane + 32 < n; // n >= 48
+			bounds(lane, lb0, ub0);
+			if (has1) bounds(lane + 32, lb1, ub1);
+			const float u0 = everywhere(lane) ? ub0 : 3e38f, u1 = has1 && everywhere(lane + 32) ? ub1 : 3e38f;
+			const uint32_t a1 = f_bits(fminf(u0, u1)), a2 = f_bits(fmaxf(u0, u1));
+			const uint32_t m1 = __reduce_min_sync(FULL, a1);
+			const uint32_t first = __ffs(__ballot_sync(FULL, a1 == m1)) - 1;
+			const float thr = bits_f(__reduce_min_sync(FULL, lane == (int)first ? a2 : a1)) * 1.001f + 1e-4f;
+			// entries inside some lane's window (y, z table cells 0 .. t*max + 1)
+			auto keep = [&](int e, float lb) { return lb <= thr && ((e >> 2) & 3) <= tymax + 1 && (e & 3) <= tzmax + 1; };
+			uint32_t s0 = __ballot_sync(FULL, keep(lane, lb0));
+			uint32_t s1 = __ballot_sync(FULL, has1 && keep(lane + 32, lb1));
+			auto visit_entry = [&](int e) {
+				const CellEntry ce = ct[e];
+				const int yy = (e >> 2) & 3, zz = e & 3, col = e >> 4;
+				// outside this lane's 3 x 3 window: no sample of the lane sees it
+				const float T = abs(yy - ty) <= 1 && abs(zz - tz) <= 1 ? ce.jx : 1e18f;
+				if ((col == 0 && split < S) || col == 3)
+					visit(BoolTag<true>(), (uint32_t)e, ce, T, col == 3 ? split : 0, col == 0 ? split : S);
+				else
+					visit(BoolTag<false>(), (uint32_t)e, ce, T, 0, S);
+			};
+			#pragma unroll 1
+			while (s0) { const int e = __ffs(s0) - 1; s0 &= s0 - 1u; visit_entry(e); }
+			#pragma unroll 1
+			while (s1) { const int e = 32 + __ffs(s1) - 1; s1 &= s1 - 1u; visit_entry(e); }
+		}
+#endif
 		#pragma unroll 1
 		for (int r = 0; r < S; r++) {
 			float Fw[2];
