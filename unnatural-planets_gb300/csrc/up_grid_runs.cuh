@@ -208,24 +208,29 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 			}
 			GX[h] = gc.x; Cc[h] = gc.y; Py[h] = pyz.x; Qy[h] = qyz.x; Pz[h] = pyz.y; Qz[h] = qyz.y;
 		}
+		// per segment: the high face minus the low one as linear functions of
+		// fx (A1 - A0 = fx DG + DC, likewise for the y and z derivatives)
+		const float DG = VALUE ? 0.f : GX[1] - GX[0], DC = VALUE ? Cc[1] - Cc[0] : (Cc[1] - GX[1]) - Cc[0];
+		const float DPy = VALUE ? 0.f : Py[1] - Py[0], DQy = VALUE ? Qy[1] - Qy[0] : (Qy[1] - Py[1]) - Qy[0];
+		const float DPz = VALUE ? 0.f : Pz[1] - Pz[0], DQz = VALUE ? Qz[1] - Qz[0] : (Qz[1] - Pz[1]) - Qz[0];
+		const float k2 = 2.f * amp * f;
 		#pragma unroll 1
 		for (; r < r1; r++) {
 			const XTab e = tab[r];
 			const float fx = e.fx;
 			const float u = e.u;
 			const float A0 = VALUE ? Cc[0] : fx * GX[0] + Cc[0];
-			const float A1 = VALUE ? Cc[1] : (fx - 1.f) * GX[1] + Cc[1];
-			const float dA = A1 - A0;
+			const float dA = VALUE ? DC : fx * DG + DC;
 			const float n = A0 + u * dA;
-			float s = n, ds = 1.f;
-			if (ridged) { s = 1.f - 2.f * fabsf(n); ds = n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f); }
+			const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
 			if (GRAD) {
 				const float du = e.du;
-				const float dnx = (VALUE ? 0.f : GX[0] + u * (GX[1] - GX[0])) + du * dA;
-				const float y0v = VALUE ? Qy[0] : fx * Py[0] + Qy[0], y1v = VALUE ? Qy[1] : (fx - 1.f) * Py[1] + Qy[1];
-				const float z0v = VALUE ? Qz[0] : fx * Pz[0] + Qz[0], z1v = VALUE ? Qz[1] : (fx - 1.f) * Pz[1] + Qz[1];
-				const float k = -amp * ds * f;
-				acc_add_fma(acc, r * stride, -amp, s, k * dnx, k * (y0v + u * (y1v - y0v)), k * (z0v + u * (z1v - z0v)));
+				const float dnx = (VALUE ? 0.f : GX[0] + u * DG) + du * dA;
+				const float y0v = VALUE ? Qy[0] : fx * Py[0] + Qy[0], dyv = VALUE ? DQy : fx * DPy + DQy;
+				const float z0v = VALUE ? Qz[0] : fx * Pz[0] + Qz[0], dzv = VALUE ? DQz : fx * DPz + DQz;
+				// -amp ds f with ds = -2 sign(n) (ridged) or 1
+				const float k = ridged ? (n > 0.f ? k2 : (n < 0.f ? -k2 : 0.f)) : -amp * f;
+				acc_add_fma(acc, r * stride, -amp, s, k * dnx, k * (y0v + u * dyv), k * (z0v + u * dzv));
 			} else {
 				acc_add_fma(acc, r * stride, -amp, s, 0.f, 0.f, 0.f);
 			}
