@@ -20,13 +20,16 @@
 // Cellular noise: in sub-runs of 8 samples, candidates outer and samples
 // inner -- each of the 3 or 4 x columns of 9 candidate cells is hashed once
 // per sub-run, a sample ignores columns outside its own 3x3x3 neighbourhood
-// (so the candidate set equals the per-sample search). The two nearest are
-// kept as integer keys (distance bits with the candidate id in the low 6
-// mantissa bits), and the winners' exact distances and difference vectors
-// are rebuilt from the ids. Values equal the per-sample kernels up to FP32
-// reassociation; the key's 2^-17 relative quantisation can only reorder
-// candidates whose distances agree to that level (F1/F2 near-ties, where
-// the gradient of F2 - F1 is discontinuous anyway).
+// (so the candidate set equals the per-sample search); with the warp's
+// shared cell table, candidates that cannot be among any sample's two
+// nearest are skipped warp-wide. The two nearest are kept as integer keys
+// (distance bits with the candidate id in the low 6 mantissa bits), and the
+// winners' distances and difference vectors are rebuilt from the ids.
+// Values equal the per-sample kernels up to FP32 reassociation and, on the
+// device, the approximate square root of the winners' distances (sqrt_hd);
+// the key's 2^-17 relative quantisation can only reorder candidates whose
+// distances agree to that level (F1/F2 near-ties, where the gradient of
+// F2 - F1 is discontinuous anyway).
 #pragma once
 #include "up_synth.cuh"
 
@@ -458,11 +461,11 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 				const float vz = (ce.jz - tzf) - fz;
 				const float vx = ce.jx - sx[r];
 				const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
-				Fw[wsel] = DIST == 0 ? sqrtf(d) : d;
+				Fw[wsel] = DIST == 0 ? sqrt_hd(d) : d;
 				vw[wsel] = v3(vx, vy, vz);
 				if (GRAD) {
 					// d F / d p for v = q - p (dv/dp = -I); Euclidean: -v / |v|
-					if (DIST == 0) dFw[wsel] = d > 0.f ? vw[wsel] * -rsqrt_hd(d) : zero3();
+					if (DIST == 0) dFw[wsel] = vw[wsel] * -(d > 0.f ? rsqrt_hd(d) : 0.f);
 					else dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
 				}
 				if (!wsel) h1 = ce.h;

@@ -53,6 +53,17 @@ UP_HD float bits_f(uint32_t u) {
 #endif
 }
 
+// square root: the hardware approximation on the device (sqrt.approx, a
+// few ulp; inputs below 2^-126 flush to 0), correctly rounded on the host
+UP_HD float sqrt_hd(float x) {
+#ifdef __CUDA_ARCH__
+	float y;
+	asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+#else
+	return sqrtf(x);
+#endif
+}
 // reciprocal square root: the hardware approximation on the device (a few
 // ulp), correctly rounded 1 / sqrt on the host; used for unit vectors only
 UP_HD float rsqrt_hd(float x) {
