@@ -78,26 +78,32 @@ UP_HD SMin smooth_min_d(float a, float b, float k, float ik) {
 	return r;
 }
 
+// Lengths and their reciprocals through sqrt_hd and rsqrt_hd: the hardware
+// approximations on the device (a few ulp), and on the host sqrtf and
+// 1 / sqrtf, the correctly rounded forms the oracle's FP32 path takes.
+UP_HD float inv_len_hd(float s) { return s > 0.f ? rsqrt_hd(s) : 0.f; } // s = squared length
 UP_HD NG torus_d(V3f p, float R, float r) {
-	const float a = sqrtf(p.x * p.x + p.y * p.y);
+	const float sa = p.x * p.x + p.y * p.y;
+	const float a = sqrt_hd(sa);
 	const float qx = a - R, qz = p.z;
-	const float ql = sqrtf(qx * qx + qz * qz);
-	const float ia = a > 0.f ? 1.f / a : 0.f, iq = ql > 0.f ? 1.f / ql : 0.f;
+	const float sq = qx * qx + qz * qz;
+	const float ql = sqrt_hd(sq);
+	const float ia = inv_len_hd(sa), iq = inv_len_hd(sq);
 	return ng(ql - r, v3(qx * iq * p.x * ia, qx * iq * p.y * ia, qz * iq));
 }
 UP_HD NG sphere_d(V3f p, V3f c, float r) {
 	const V3f d = p - c;
-	const float l = length(d);
-	return ng(l - r, l > 0.f ? d * (1.f / l) : zero3());
+	const float s = dot(d, d);
+	return ng(sqrt_hd(s) - r, d * inv_len_hd(s));
 }
 UP_HD NG box_d(V3f p, float h, float rr) {
 	const V3f q = v3(fabsf(p.x) - h, fabsf(p.y) - h, fabsf(p.z) - h);
 	const V3f m = v3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
-	const float ml = length(m);
+	const float ml = sqrt_hd(dot(m, m));
 	const float mx = fmaxf(q.x, fmaxf(q.y, q.z));
 	const V3f sg = v3(p.x >= 0.f ? 1.f : -1.f, p.y >= 0.f ? 1.f : -1.f, p.z >= 0.f ? 1.f : -1.f);
 	V3f g;
-	if (ml > 0.f) g = v3(sg.x * m.x, sg.y * m.y, sg.z * m.z) * (1.f / ml);
+	if (ml > 0.f) g = v3(sg.x * m.x, sg.y * m.y, sg.z * m.z) * inv_len_hd(dot(m, m));
 	else if (q.x >= q.y && q.x >= q.z) g = v3(sg.x, 0.f, 0.f);
 	else if (q.y >= q.z) g = v3(0.f, sg.y, 0.f);
 	else g = v3(0.f, 0.f, sg.z);
