@@ -374,7 +374,9 @@ def extra_batch(up, W, stream):
 def extra_fit(up, W, stream, steps=300):
     """inverse fit of the torus + spheres - ridged Perlin + cellular planet:
     theta* = the program's 25 parameters scaled by (1 + 0.05 U[-1,1]) from
-    seed 1, theta0 = theta* scaled by (1 + 0.05 U[-1,1]) from seed 2"""
+    seed 1, theta0 = theta* scaled by (1 + 0.05 s U[-1,1]) from seed 2, with
+    s the phase scale (f_min / f for octave frequencies, 1 otherwise); Adam
+    moves u in theta = theta0 (1 + s u)"""
     import numpy as np
     import torch
     from oracle import oracle as O
@@ -382,7 +384,7 @@ def extra_fit(up, W, stream, steps=300):
     P = W.torus_spheres_ridged_cellular()
     base = W.theta_of(P).astype(np.float64)
     t_star_np = (base * (1 + 0.05 * np.random.default_rng(1).uniform(-1, 1, size=base.shape))).astype(np.float32)
-    t0 = (t_star_np * (1 + 0.05 * np.random.default_rng(2).uniform(-1, 1, size=base.shape))).astype(np.float32)
+    t0 = (t_star_np * (1 + 0.05 * W.phase_scale(P, t_star_np) * np.random.default_rng(2).uniform(-1, 1, size=base.shape))).astype(np.float32)
     t_star = torch.from_numpy(t_star_np).cuda()
     target = up.Planet(program=P)
     target.set_stream(stream.cuda_stream)
@@ -393,7 +395,8 @@ def extra_fit(up, W, stream, steps=300):
     xg = AG.grid_positions(gg)  # the grid kernel's sample positions
     d_star = target.sdf_points(x, d=torch.empty(n, device="cuda"))
     s_star = torch.sign(target.sdf_points(xg, d=torch.empty(xg.shape[0], device="cuda")))
-    rel = AG.RelativeTheta(torch.tensor(t0, device="cuda"))   # theta = theta0 (1 + u), Adam moves u
+    # theta = theta0 (1 + s u), Adam moves u; s: phase scale of theta0
+    rel = AG.RelativeTheta(torch.tensor(t0, device="cuda"), torch.from_numpy(W.phase_scale(P, t0)).cuda())
     planet = up.Planet(program=W.torus_spheres_ridged_cellular())
     planet.set_stream(stream.cuda_stream)
     opt = torch.optim.Adam(rel.parameters(), lr=1e-2)
@@ -420,13 +423,7 @@ def extra_fit(up, W, stream, steps=300):
     fit = planet.sdf_points(xs)
     ref = O.synth_points(P, xs, theta=t_star_np.astype(np.float64))
     # relative error per parameter group (layout of workloads.theta_of)
-    amp_i, freq_i, o = [], [], 0
-    for l in range(P.n_layers):
-        k = P.layer[l].octaves
-        amp_i += list(range(o, o + k))
-        freq_i += list(range(o + k, o + 2 * k))
-        o += 2 * k
-    groups = {"amplitudes": amp_i, "frequencies": freq_i, "shape": list(range(o, len(t_star_np)))}
+    groups = W.theta_groups(P)
 
     def group_err(t):
         t = np.asarray(t, np.float64)
@@ -436,9 +433,10 @@ def extra_fit(up, W, stream, steps=300):
             "theta_rel_err_by_group_start": group_err(t0), "theta_rel_err_by_group_end": group_err(theta.detach().cpu().numpy()),
             "sdf_rms_vs_fp64_oracle": float(np.sqrt(np.mean((fit - ref) ** 2))),
             "what": "torus + 8 spheres - ridged perlin + cellular, 25 parameters; theta* = theta (1 + 0.05 U) seed 1, "
-                    "theta0 = theta* (1 + 0.05 U) seed 2; L = mean((d - d*)^2) on 32M points of the 0.05 shell (Morton order) + "
-                    "mean(relu(-d sign(d*))) on 256^3 (forward through the grid kernel); Adam lr 1e-2 on the relative parameters u, "
-                    "theta = theta0 (1 + u); SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
+                    "theta0 = theta* (1 + 0.05 s U) seed 2 with s = f_min / f for octave frequencies (phase scale), 1 otherwise; "
+                    "L = mean((d - d*)^2) on 32M points of the 0.05 shell (Morton order) + "
+                    "mean(relu(-d sign(d*))) on 256^3 (forward through the grid kernel); Adam lr 1e-2 on u, "
+                    "theta = theta0 (1 + s u); SDF RMS against the FP64 oracle at theta* on 65536 shell points"}
 
 
 def extra_modes(up, stream):

@@ -77,21 +77,32 @@ def grid_positions(grid, device="cuda") -> torch.Tensor:
 
 
 class RelativeTheta(torch.nn.Module):
-    """theta = theta0 * (1 + u), with u the parameter an optimiser moves.
+    """theta = theta0 * (1 + scale * u), with u the parameter an optimiser moves.
 
     The program's parameters span five orders of magnitude (octave amplitudes
     of 6e-4, frequencies up to 96, radii near 1). An optimiser step of fixed
     size in theta overshoots the small ones and barely moves the large ones;
     in u every parameter moves in units of its own starting size. Entries of
-    theta0 that are 0 cannot move."""
+    theta0 that are 0 cannot move.
 
-    def __init__(self, theta0: torch.Tensor):
+    scale (default 1) sets each parameter's unit further. With
+    workloads.phase_scale a frequency f moves in units of f_min / f of itself:
+    one unit shifts every octave's noise by the same number of lattice cells
+    at a given point. The loss is only locally convex in a frequency (the
+    noise at p decorrelates once the frequency error times |p| reaches about
+    one cell, 0.7 % at f = 96 and |p| = 1.4), so equal relative steps (an Adam
+    step of lr = 1e-2 moves every u by about 1e-2) throw the high octaves out
+    of their basins in the first steps."""
+
+    def __init__(self, theta0: torch.Tensor, scale: torch.Tensor | None = None):
         super().__init__()
         self.register_buffer("theta0", theta0.detach().clone())
+        s = torch.ones_like(self.theta0) if scale is None else scale.detach().to(self.theta0).clone()
+        self.register_buffer("scale", s)
         self.u = torch.nn.Parameter(torch.zeros_like(self.theta0))
 
     def forward(self) -> torch.Tensor:
-        return self.theta0 * (1 + self.u)
+        return self.theta0 * (1 + self.scale * self.u)
 
 
 def _theta_of(planet):

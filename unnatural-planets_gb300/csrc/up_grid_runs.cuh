@@ -463,11 +463,8 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 				const float d = cell_metric<DIST>(vx, vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
 				Fw[wsel] = DIST == 0 ? sqrt_hd(d) : d;
 				vw[wsel] = v3(vx, vy, vz);
-				if (GRAD) {
-					// d F / d p for v = q - p (dv/dp = -I); Euclidean: -v / |v|
-					if (DIST == 0) dFw[wsel] = vw[wsel] * -(d > 0.f ? rsqrt_hd(d) : 0.f);
-					else dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
-				}
+				// d F / d p for v = q - p (dv/dp = -I); Euclidean: -v / |v|
+				if (GRAD) dFw[wsel] = cell_dist_grad(vw[wsel], d, DIST);
 				if (!wsel) h1 = ce.h;
 			}
 			const float a = Fw[0], b = Fw[1];

@@ -348,8 +348,10 @@ UP_HD float jitter(uint32_t h, int s) { return bits_f(0x3F800000u | (((h >> s) &
 
 UP_HD float signf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
 // gradient with respect to p of the distance metric of v = q - p
+// (Euclidean: F is the squared distance here; -v / |v| with the reciprocal
+// square root of rsqrt_hd, 1 / sqrtf on the host)
 UP_HD V3f cell_dist_grad(V3f v, float F, int dist) {
-	if (dist == 0) return F > 0.f ? v * (-1.f / F) : zero3();
+	if (dist == 0) return v * -(F > 0.f ? rsqrt_hd(F) : 0.f);
 	const V3f sg = v3(signf(v.x), signf(v.y), signf(v.z));
 	if (dist == 1) return -sg;
 	return -(v * 2.f + sg);
@@ -412,14 +414,14 @@ UP_HD NG cellular_n(V3f p, uint32_t key, int dist_rt, int op_rt) {
 		g[w] = v3(vx, vy, vz);
 		if (w == 0) cellh = h;
 	}
-	float F1 = F[0], F2 = F[1];
-	if (dist == 0) { F1 = sqrtf(F1); F2 = sqrtf(F2); }
 	// d F / d p for the stored difference vectors v = q - p (dv/dp = -I)
 	V3f dF1 = zero3(), dF2 = zero3();
 	if (GRAD) {
-		dF1 = cell_dist_grad(g[0], F1, dist);
-		dF2 = cell_dist_grad(g[1], F2, dist);
+		dF1 = cell_dist_grad(g[0], F[0], dist);
+		dF2 = cell_dist_grad(g[1], F[1], dist);
 	}
+	float F1 = F[0], F2 = F[1];
+	if (dist == 0) { F1 = sqrt_hd(F1); F2 = sqrt_hd(F2); }
 	switch (op) {
 		case 0: return ngc(hash_signed(mix32(cellh)));
 		case 1: return ng(F1 - 1.f, dF1);
@@ -497,13 +499,13 @@ __device__ NG cellular_warp(V3f p, uint32_t key, int dist_rt, int op_rt) {
 		g[w] = v3(vx, vy, vz);
 		if (w == 0) cellh = __float_as_uint(t.w);
 	}
-	float F1 = F[0], F2 = F[1];
-	if (dist == 0) { F1 = sqrtf(F1); F2 = sqrtf(F2); }
 	V3f dF1 = zero3(), dF2 = zero3();
 	if (GRAD) {
-		dF1 = cell_dist_grad(g[0], F1, dist);
-		dF2 = cell_dist_grad(g[1], F2, dist);
+		dF1 = cell_dist_grad(g[0], F[0], dist);
+		dF2 = cell_dist_grad(g[1], F[1], dist);
 	}
+	float F1 = F[0], F2 = F[1];
+	if (dist == 0) { F1 = sqrt_hd(F1); F2 = sqrt_hd(F2); }
 	switch (op) {
 		case 0: return ngc(hash_signed(mix32(cellh)));
 		case 1: return ng(F1 - 1.f, dF1);

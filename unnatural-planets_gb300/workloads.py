@@ -114,6 +114,34 @@ def theta_of(P: abi.SynthProgram) -> np.ndarray:
     return np.asarray(t, dtype=np.float32)
 
 
+def theta_groups(P: abi.SynthProgram) -> dict:
+    """Indices of theta_of's vector by kind: octave amplitudes, octave
+    frequencies and the base shape's parameters."""
+    amp, freq, o = [], [], 0
+    for l in range(P.n_layers):
+        k = P.layer[l].octaves
+        amp += list(range(o, o + k))
+        freq += list(range(o + k, o + 2 * k))
+        o += 2 * k
+    return {"amplitudes": amp, "frequencies": freq, "shape": list(range(o, len(theta_of(P))))}
+
+
+def phase_scale(P: abi.SynthProgram, theta: np.ndarray | None = None) -> np.ndarray:
+    """Per-parameter unit of relative change in phase terms: f_min / f_i for
+    every octave frequency f_i of theta (theta_of(P) by default; f_min the
+    smallest of them), 1 for amplitudes and the base shape. A relative change
+    of one unit in frequency i then moves the noise at a point by the same
+    number of lattice cells for every octave (autograd.RelativeTheta)."""
+    t = theta_of(P) if theta is None else np.asarray(theta, np.float32)
+    s = np.ones(len(t), np.float32)
+    fi = theta_groups(P)["frequencies"]
+    if fi:
+        fmin = float(np.min(np.abs(t[fi])))
+        for i in fi:
+            s[i] = fmin / abs(float(t[i])) if t[i] != 0 else 1.0
+    return s
+
+
 def shell_points(P_radius: float, thickness: float, n: int, seed: int) -> np.ndarray:
     """n points uniform in the spherical shell |p| in [R - t, R + t]."""
     rng = np.random.default_rng(seed)
