@@ -23,9 +23,9 @@ each ("extras" in the JSON line, each bounded to seconds):
   batch      64 planets x 512 uneven chunks (1.8e8 samples): one batched
              call (graph replay) against one up_contour call per chunk
   fit        inverse fit of that program's 25 parameters, 300 Adam steps
-             (lr 1e-2) on 32M shell points plus a sign loss on the 256^3
-             grid; reports |theta - theta*| and the SDF RMS against the
-             FP64 oracle
+             (lr 1e-2, octave frequencies in phase units) on 32M shell points
+             plus a sign loss on the 256^3 grid; reports |theta - theta*| by
+             parameter group and the SDF RMS against the FP64 oracle
   modes      reference-mode planet sphere/lakes/default, seed 0, 500^3 over
              [-2000, 2000]^3, land+water+navigation in one pass
   cpu_1t     the CPU baseline on one thread
@@ -50,14 +50,14 @@ METRIC = "SDF+grad Gsamples/s at 512^3 (fused value+gradient; plain and ms/plane
 UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
-# capture of synth_grid_runs_kernel<1,2,1301> at 256^3 (0.256 MB + 244.18 MB
-# over 16,777,216 samples)
-TRAFFIC_PER_SAMPLE_FUSED = 244.438528e6 / 16777216
+# capture of the timed synth_grid_runs_kernel<1,2,1301> launch at 512^3
+# (3.07 MB + 2,413.63 MB over 134,217,728 samples)
+TRAFFIC_PER_SAMPLE_FUSED = 2416.704e6 / 134217728
 # FP32 operations executed per sample by the fused grid kernel (FFMA x 2,
 # FFMA2 x 4, FADD, FMUL per thread instruction) and its thread instructions per
 # sample, from the ncu instruction counts of the same capture
-EXEC_FP32_PER_SAMPLE_FUSED = 754.9
-INSTR_PER_SAMPLE_FUSED = 1162.4
+EXEC_FP32_PER_SAMPLE_FUSED = 528.2
+INSTR_PER_SAMPLE_FUSED = 797.2
 
 
 def workload_config(grid: int, n: int) -> dict:
@@ -659,8 +659,9 @@ def run_ours(args) -> None:
                 "what": "up_sdf_grid value+gradient into pinned host buffers"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "traffic": TRAFFIC_PER_SAMPLE_FUSED * N,
-                     "traffic_source": "dram read+write of synth_grid_runs_kernel<1,2,1301> from one ncu capture at 256^3 "
-                                       f"({TRAFFIC_PER_SAMPLE_FUSED:.2f} B/sample), scaled by samples to this launch",
+                     "traffic_source": "dram read+write of the timed synth_grid_runs_kernel<1,2,1301> launch from one ncu "
+                                       f"capture of this workload at 512^3 ({TRAFFIC_PER_SAMPLE_FUSED:.2f} B/sample: writes of 16 B "
+                                       "per sample and about 12 % more, no re-reads), per sample times this launch's samples",
                      "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x {max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)",
                      "flops_per_sample": W.FLOPS_PER_SAMPLE_C2,
                      "flops_definition": "value path, counted by the oracle's operation-counting FP32 scalar (FMA = 2)",
@@ -675,10 +676,11 @@ def run_ours(args) -> None:
                                    "achieved": EXEC_FP32_PER_SAMPLE_FUSED * N / (t_fused * 1e-3) / 1e12,
                                    "frac": EXEC_FP32_PER_SAMPLE_FUSED * N / (t_fused * 1e-3) / 1e12 / fp32_peak,
                                    "source": "FP32 operations the fused kernel executes per sample (FFMA and FFMA2 lanes x 2, FADD, "
-                                             "FMUL), from the ncu instruction counts at 256^3 (profiles/)"},
-                     "note": "the kernel is instruction-issue bound (about 80 % issue active): per sample it issues about "
-                             f"{INSTR_PER_SAMPLE_FUSED:.0f} thread instructions, of which the cellular candidate keys (integer "
-                             "min/max, bit masks) and control flow are a large share; see profiles/",                     "hbm_view": {"algorithmic_bytes": 16 * N, "achieved_gbs": 16 * N / (t_fused * 1e-3) / 1e9,
+                                             "FMUL), from the ncu instruction counts of this workload at 512^3 (profiles/)"},
+                     "note": "the kernel is instruction-issue bound (about 84 % issue active): per sample it issues about "
+                             f"{INSTR_PER_SAMPLE_FUSED:.0f} thread instructions, of which the lattice hashes and face setup of the "
+                             "Perlin octaves, the cellular keys (integer min/max, bit masks), addressing and control flow are "
+                             "the non-FP32 share; see profiles/",                     "hbm_view": {"algorithmic_bytes": 16 * N, "achieved_gbs": 16 * N / (t_fused * 1e-3) / 1e9,
                                   "peak_gbs": peaks.get("hbm_gbs"), "frac": (16 * N / (t_fused * 1e-3) / 1e9) / peaks["hbm_gbs"]
                                   if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}},
         "cpu_baseline": {"value": cpu_grad / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
