@@ -139,7 +139,8 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 	const float dWy[4] = {-dv * (1.f - w), dv * (1.f - w), -dv * w, dv * w};
 	const float dWz[4] = {-(1.f - v) * dw, -v * dw, (1.f - v) * dw, v * dw};
 	const uint32_t y0 = (uint32_t)iy * HY, z0 = ((uint32_t)iz * HZ) ^ key, z1 = ((uint32_t)iz * HZ + HZ) ^ key;
-	const uint32_t yz[4] = {y0 ^ z0, (y0 + HY) ^ z0, y0 ^ z1, (y0 + HY) ^ z1};
+	// the y/z half of each corner's hash, its first mixing step applied
+	const uint32_t yz[4] = {mix32_head(y0 ^ z0), mix32_head((y0 + HY) ^ z0), mix32_head(y0 ^ z1), mix32_head((y0 + HY) ^ z1)};
 	const float ys[4] = {fy, fy - 1.f, fy, fy - 1.f}, zs[4] = {fz, fz, fz - 1.f, fz - 1.f};
 	// starts: bit r set when sample r begins a segment (its x cell differs
 	// from sample r - 1's), the same for every lane
@@ -181,11 +182,11 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 		#pragma unroll
 		for (int h = 0; h < 2; h++) {
 			if (h == 0 && carry) continue;
-			const uint32_t xh = (uint32_t)(cx + h) * HX;
+			const uint32_t xh = mix32_head((uint32_t)(cx + h) * HX);
 			V3f cg[4]; // corner c: gradient vector, or the value in .x
 			#pragma unroll
 			for (int c = 0; c < 4; c++) {
-				const uint32_t hh = mix32(xh ^ yz[c]);
+				const uint32_t hh = mix32_tail(xh ^ yz[c]); // == mix32(x part ^ y/z part)
 				cg[c] = VALUE ? v3(hash_signed(hh), 0.f, 0.f) : grad_lookup(hh);
 			}
 			// the face's coefficients, summed over its 4 corners in pairs:
@@ -232,7 +233,7 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 				const float y0v = VALUE ? Qy[0] : fx * Py[0] + Qy[0], dyv = VALUE ? DQy : fx * DPy + DQy;
 				const float z0v = VALUE ? Qz[0] : fx * Pz[0] + Qz[0], dzv = VALUE ? DQz : fx * DPz + DQz;
 				// -amp ds f with ds = -2 sign(n) (ridged) or 1
-				const float k = ridged ? (n > 0.f ? k2 : (n < 0.f ? -k2 : 0.f)) : -amp * f;
+				const float k = ridged ? (n != 0.f ? mul_sign(k2, n) : 0.f) : -amp * f;
 				acc_add_fma(acc, r * stride, -amp, s, k * dnx, k * (y0v + u * dyv), k * (z0v + u * dzv));
 			} else {
 				acc_add_fma(acc, r * stride, -amp, s, 0.f, 0.f, 0.f);
@@ -482,8 +483,7 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			}
 			// ridged: s = 1 - 2|n|, selected without a branch
 			const float s = ridged ? 1.f - 2.f * fabsf(n) : n;
-			const float ds = ridged ? (n > 0.f ? -2.f : (n < 0.f ? 2.f : 0.f)) : 1.f;
-			const float k = -amp * ds * f;
+			const float k = ridged ? (n != 0.f ? mul_sign(2.f * amp * f, n) : 0.f) : -amp * f;
 			acc_add(acc, (r0 + r) * stride, -amp * s, k * dn.x, k * dn.y, k * dn.z);
 		}
 	};

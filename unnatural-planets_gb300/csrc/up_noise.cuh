@@ -138,6 +138,14 @@ UP_HD uint32_t mix32(uint32_t x) {
 	x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
 	return x;
 }
+// mix32 in two parts: its first step distributes over xor (a logical shift
+// does), so mix32(a ^ b) == mix32_tail(mix32_head(a) ^ mix32_head(b)), and a
+// caller that hashes many a ^ b with a shared b forms mix32_head(b) once
+UP_HD uint32_t mix32_head(uint32_t x) { return x ^ (x >> 16); }
+UP_HD uint32_t mix32_tail(uint32_t x) {
+	x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+	return x;
+}
 UP_HD uint32_t seed_key(uint32_t seed) { return mix32(seed + 0x9E3779B9U); }
 constexpr uint32_t HX = 73856093U, HY = 19349663U, HZ = 83492791U;
 UP_HD uint32_t lattice_hash(int ix, int iy, int iz, uint32_t key) {
@@ -347,6 +355,8 @@ UP_HD NG simplex_n(V3f p, uint32_t key) {
 UP_HD float jitter(uint32_t h, int s) { return bits_f(0x3F800000u | (((h >> s) & 1023U) << 13)) - 0.99951171875f; }
 
 UP_HD float signf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+// x with its sign flipped when s is negative: x sign(s) for s != 0, +-x for s = +-0
+UP_HD float mul_sign(float x, float s) { return bits_f(f_bits(x) ^ (f_bits(s) & 0x80000000u)); }
 // gradient with respect to p of the distance metric of v = q - p
 // (Euclidean: F is the squared distance here; -v / |v| with the reciprocal
 // square root of rsqrt_hd, 1 / sqrtf on the host)
