@@ -218,7 +218,11 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 		const float DPy = VALUE ? 0.f : Py[1] - Py[0], DQy = VALUE ? Qy[1] - Qy[0] : (Qy[1] - Py[1]) - Qy[0];
 		const float DPz = VALUE ? 0.f : Pz[1] - Pz[0], DQz = VALUE ? Qz[1] - Qz[0] : (Qz[1] - Pz[1]) - Qz[0];
 		const float k2 = 2.f * amp * f;
-		#pragma unroll 1
+		// two samples per step in the reference-mode instantiation (RIDGED < 0:
+		// value only, several noise instances per kernel), one elsewhere (both
+		// measured fastest for their kernel)
+		constexpr int SAMPLE_UNROLL = RIDGED < 0 ? 2 : 1;
+		#pragma unroll SAMPLE_UNROLL
 		for (; r < r1; r++) {
 			const XTab e = tab[r];
 			const float fx = e.fx;
@@ -449,7 +453,7 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			while (s1) { const int e = 32 + __ffs(s1) - 1; s1 &= s1 - 1u; visit_entry(e); }
 		}
 #endif
-		#pragma unroll 1
+		#pragma unroll 2
 		for (int r = 0; r < S; r++) {
 			float Fw[2];
 			V3f vw[2], dFw[2] = {zero3(), zero3()};
