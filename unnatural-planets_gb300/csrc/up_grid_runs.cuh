@@ -437,20 +437,25 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			auto keep = [&](int e, float lb) { return lb <= thr && ((e >> 2) & 3) <= tymax + 1 && (e & 3) <= tzmax + 1; };
 			uint32_t s0 = __ballot_sync(FULL, keep(lane, lb0));
 			uint32_t s1 = __ballot_sync(FULL, has1 && keep(lane + 32, lb1));
-			auto visit_entry = [&](int e) {
-				const CellEntry ce = ct[e];
-				const int yy = (e >> 2) & 3, zz = e & 3, col = e >> 4;
-				// outside this lane's 3 x 3 window: no sample of the lane sees it
-				const float T = abs(yy - ty) <= 1 && abs(zz - tz) <= 1 ? ce.jx : 1e18f;
-				if ((col == 0 && split < S) || col == 3)
-					visit(BoolTag<true>(), (uint32_t)e, ce, T, col == 3 ? split : 0, col == 0 ? split : S);
-				else
-					visit(BoolTag<false>(), (uint32_t)e, ce, T, 0, S);
+			// survivors of the 16 entries of column col (bits of m), all seen by
+			// samples [rlo, rhi) only (MASKED) or by every sample
+			auto visit_col = [&](auto masked_tag, uint32_t m, int col, int rlo, int rhi) {
+				#pragma unroll 1
+				while (m) {
+					const int e = col * 16 + __ffs(m) - 1;
+					m &= m - 1u;
+					const CellEntry ce = ct[e];
+					const int yy = (e >> 2) & 3, zz = e & 3;
+					// outside this lane's 3 x 3 window: no sample of the lane sees it
+					const float T = abs(yy - ty) <= 1 && abs(zz - tz) <= 1 ? ce.jx : 1e18f;
+					visit(masked_tag, (uint32_t)e, ce, T, rlo, rhi);
+				}
 			};
-			#pragma unroll 1
-			while (s0) { const int e = __ffs(s0) - 1; s0 &= s0 - 1u; visit_entry(e); }
-			#pragma unroll 1
-			while (s1) { const int e = 32 + __ffs(s1) - 1; s1 &= s1 - 1u; visit_entry(e); }
+			// column 0 serves the samples of cell ixa, column 3 those of ixa + 1
+			if (split < S) visit_col(BoolTag<true>(), s0 & 0xFFFFu, 0, 0, split);
+			else visit_col(BoolTag<false>(), s0 & 0xFFFFu, 0, 0, S);
+			visit_col(BoolTag<false>(), (s0 >> 16) | ((s1 & 0xFFFFu) << 16), 1, 0, S); // columns 1 and 2
+			visit_col(BoolTag<true>(), s1 >> 16, 3, split, S);
 		}
 #endif
 		#pragma unroll 2
