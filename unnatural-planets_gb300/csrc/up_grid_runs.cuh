@@ -24,9 +24,13 @@
 // shared cell table, candidates that cannot be among any sample's two
 // nearest are skipped warp-wide. The two nearest are kept as integer keys
 // (distance bits with the candidate id in the low 6 mantissa bits), and the
-// winners' distances and difference vectors are rebuilt from the ids.
-// Values equal the per-sample kernels up to FP32 reassociation and, on the
-// device, the approximate square root of the winners' distances (sqrt_hd);
+// winners' distances and difference vectors are rebuilt from the ids (the
+// value-only form on the device takes the winners' metrics from the keys
+// themselves, the middle of their 2^-17 relative quantum, and rebuilds
+// nothing). Values equal the per-sample kernels up to FP32 reassociation
+// and, on the device, the approximate square root of the winners' distances
+// (sqrt_hd) and the value-only form's quantised metrics (within 2^-18
+// relative; 1e-7 of the benchmark planet's value);
 // the key's 2^-17 relative quantisation can only reorder candidates whose
 // distances agree to that level (F1/F2 near-ties, where the gradient of
 // F2 - F1 is discontinuous anyway).
@@ -465,6 +469,15 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			uint32_t h1 = 0;
 			#pragma unroll
 			for (int wsel = 0; wsel < 2; wsel++) {
+#ifdef __CUDA_ARCH__
+				if (!GRAD && OP != 0) {
+					// value only (device): the winner's metric from its key, the
+					// middle of the key's 2^-17 relative quantum; no rebuild
+					const float d = bits_f(((wsel ? K2[r] : K1[r]) & ~63u) | 32u);
+					Fw[wsel] = DIST == 0 ? sqrt_hd(d) : d;
+					continue;
+				}
+#endif
 				const int id = (int)((wsel ? K2[r] : K1[r]) & 63u);
 				const CellEntry ce = cand(id);
 				const float vy = (ce.jy - tyf) - fy;
