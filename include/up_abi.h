@@ -337,8 +337,10 @@ int up_sdf_param_backward(up_context *ctx, const float *points, size_t n, const 
  * until the process exits; the kernel never launches more than 2048 blocks,
  * so any point count fits, and a parameter vector longer than 43 entries is
  * rejected. Creating the context looks up the array's device address (with
- * the context's device current), so the call itself makes no runtime query.
- * All calls share the array: calls that overlap on the GPU race. */
+ * the context's device current), so the call itself makes no runtime query;
+ * after a device reset (cudaDeviceReset) that address is gone with the old
+ * device state, so create a new context. All calls share the array: calls
+ * that overlap on the GPU race. */
 int up_sdf_param_backward_noalloc(up_context *ctx, const float *points, size_t n, const float *dL_dd, float *dtheta);
 
 /* ---------------------------------------------------------------- batching */
