@@ -1,7 +1,7 @@
 """GPU parity of the reference modes (34 shapes, 6 elevation modes, 5
 fields) through the C ABI.
 
-Tolerances (the benchmark spec: SDF error <= 1e-5 relative to the FP64 oracle, taken
+Tolerances (the path's bar: SDF error <= 1e-5 relative to the FP64 oracle, taken
 relative to the planets' shape scale, the sphere radius R = 1100 of
 sdf.cpp:20-23, so 0.011 in the planets' units):
   - against FP64, at least 99.9 % of the samples of every shape and every

@@ -12,7 +12,7 @@ the texels of textures.cpp:24-43).
                  contouring of the value-only GPU grid
   atlas          the 4096^2 texel atlas of that mesh, every texel
 
-Tolerances (the benchmark spec bar, written here):
+Tolerances (the path's accuracy bar, written here):
   SDF value      |GPU - FP64| <= 1e-5 (unit-scale planets) for every checked sample
   gradient       |GPU - FP64| <= 1e-4 max(1, |grad|) for all but 1e-4 of the
                  samples (cellular F1/F2 swaps and the ridged |n| kink are

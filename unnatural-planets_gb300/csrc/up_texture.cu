@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(256) tex_dilate_fused_kernel(const float *__re
 				for (int dx = -1; dx <= 1; dx++) {
 					if (!dx && !dy) continue;
 					const int ni = (ly + dy) * SX + lx + dx;
-					if (tag[ni] >= k) continue; // not valid before this round (or absent)
+					if (tag[ni] >= k) continue; // not valid before this dilation pass (or absent)
 					const float *r = A + ni * NS;
 					for (int c = 0; c < nch; c++) acc[c] += r[c];
 					cnt++;
