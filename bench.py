@@ -135,10 +135,11 @@ def cpu_planet(P, grid, threads: int) -> dict:
 
 def error_vs_fp64(up, W, planet, P, grid, d_dev, g_dev, mesh, threads: int) -> dict:
     """Error of each result against the FP64 oracle (a checker run after the
-    timed regions): SDF values and gradients at 2^20 seeded grid points of the
-    512^3 grid, every vertex of the planet's mesh against the oracle's
-    contouring of the same FP32 grid, and every covered texel of the 4096^2
-    atlas of that mesh."""
+    timed regions): SDF values (d_dev: the value-only form's grid, the last one
+    sampled) and gradients (g_dev: the fused form's) at 2^20 seeded grid points
+    of the 512^3 grid, every vertex of the planet's mesh against the oracle's
+    contouring of that FP32 grid, and every covered texel of the 4096^2 atlas
+    of that mesh."""
     import numpy as np
     import torch
     from oracle import oracle as O
