@@ -135,11 +135,11 @@ def cpu_planet(P, grid, threads: int) -> dict:
 
 def error_vs_fp64(up, W, planet, P, grid, d_dev, g_dev, mesh, threads: int) -> dict:
     """Error of each result against the FP64 oracle (a checker run after the
-    timed regions): SDF values (d_dev: the value-only form's grid, the last one
-    sampled) and gradients (g_dev: the fused form's) at 2^20 seeded grid points
-    of the 512^3 grid, every vertex of the planet's mesh against the oracle's
-    contouring of that FP32 grid, and every covered texel of the 4096^2 atlas
-    of that mesh."""
+    timed regions): SDF values of both forms (d_dev holds the value-only grid,
+    the last one sampled; the fused grid is sampled once more) and the fused
+    gradients at 2^20 seeded grid points of the 512^3 grid, every vertex of the
+    planet's mesh against the oracle's contouring of the value-only FP32 grid,
+    and every covered texel of the 4096^2 atlas of that mesh."""
     import numpy as np
     import torch
     from oracle import oracle as O
@@ -148,9 +148,18 @@ def error_vs_fp64(up, W, planet, P, grid, d_dev, g_dev, mesh, threads: int) -> d
     it = torch.from_numpy(idx).cuda()
     dv = d_dev[it].double().cpu().numpy()
     gv = torch.stack([g_dev[it], g_dev[n + it], g_dev[2 * n + it]], dim=1).double().cpu().numpy()
+    # the fused form's own values at the same points: the grid is sampled once
+    # more with gradients, then value-only again (the grid the mesh is checked on)
+    planet.sdf_grid(grid, 1, outs=[d_dev, None, None], grad=g_dev)
+    dvf = d_dev[it].double().cpu().numpy()
+    planet.sdf_grid(grid, 1, outs=[d_dev, None, None])
     ref, rg = O.synth_points(P, O.grid_positions_at(grid, idx), grad=True, threads=threads)
-    ev, eg = np.abs(dv - ref), np.abs(gv - rg).max(axis=1) / np.maximum(1.0, np.abs(rg).max(axis=1))
-    out = {"value": {"max": float(ev.max()), "rms": float(np.sqrt((ev ** 2).mean())), "samples": int(len(idx)), "tolerance": 1e-5},
+    ev, evf = np.abs(dv - ref), np.abs(dvf - ref)
+    eg = np.abs(gv - rg).max(axis=1) / np.maximum(1.0, np.abs(rg).max(axis=1))
+    out = {"value": {"max": float(ev.max()), "rms": float(np.sqrt((ev ** 2).mean())), "samples": int(len(idx)), "tolerance": 1e-5,
+                     "form": "value only"},
+           "value_fused": {"max": float(evf.max()), "rms": float(np.sqrt((evf ** 2).mean())), "samples": int(len(idx)),
+                           "tolerance": 1e-5, "form": "value + gradient"},
            "gradient": {"max_rel": float(eg.max()), "rms_rel": float(np.sqrt((eg ** 2).mean())),
                         "frac_above_1e-4": float((eg > 1e-4).mean()), "samples": int(len(idx))}}
     pos, nrm, tri = mesh
