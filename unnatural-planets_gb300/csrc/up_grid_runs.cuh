@@ -136,8 +136,16 @@ UP_HD void lattice_octave_run_t(const RunCtx &rc, int R, float f, float amp, uin
 	const float fy0 = floorf(qy), fz0 = floorf(qz);
 	const int iy = (int)fy0, iz = (int)fz0;
 	const float fy = qy - fy0, fz = qz - fz0;
-	const float v = fade(fy), w = fade(fz);
-	const float dv = GRAD ? dfade(fy) : 0.f, dw = GRAD ? dfade(fz) : 0.f;
+	// fade and fade' of y and z as FP32 pairs: t^3 (t (6 t - 15) + 10) and
+	// 30 t^2 (t (t - 2) + 1)
+	const P2 t = p2(fy, fz), t2 = mul2(t, t);
+	const P2 fd = mul2(mul2(t2, t), fma2(t, fma2(t, p2s(6.f), p2s(-15.f)), p2s(10.f)));
+	const float v = fd.x, w = fd.y;
+	float dv = 0.f, dw = 0.f;
+	if (GRAD) {
+		const P2 dd = mul2(mul2(p2s(30.f), t2), fma2(t, add2(t, p2s(-2.f)), p2s(1.f)));
+		dv = dd.x; dw = dd.y;
+	}
 	// y/z corners c = by + 2 bz
 	const float Wyz[4] = {(1.f - v) * (1.f - w), v * (1.f - w), (1.f - v) * w, v * w};
 	const float dWy[4] = {-dv * (1.f - w), dv * (1.f - w), -dv * w, dv * w};
@@ -666,7 +674,7 @@ __device__ __forceinline__ void runs_task_signs(uint32_t *__restrict__ signs, ui
 // samples, which has their sign, without evaluating the base per sample.
 template<bool GRAD, int T0, int T1>
 UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typename AccOf<GRAD>::T *acc, int stride, float band = 0.f) {
-	bool far = band > 0.f;
+	bool far = !GRAD && band > 0.f; // the narrow band is a value-only mode
 	const float x0 = rc.px(0), x1 = rc.px(R - 1);
 	const uint32_t spheres = synth_segment_spheres(P, x0, x1, rc.py, rc.pz);
 	bool filled = false;
@@ -696,7 +704,7 @@ UP_HD void synth_run(const up_synth_program &P, const RunCtx &rc, int R, typenam
 		default: base_loop(IntTag<UP_BASE_TORUS_SPHERES>()); break;
 	}
 #ifdef __CUDA_ARCH__
-	far = __all_sync(0xFFFFFFFFu, far); // every lane of the warp runs every task
+	if (!GRAD) far = __all_sync(0xFFFFFFFFu, far); // every lane of the warp runs every task
 #endif
 	if (far) return;
 	if (P.n_layers > 0) layer_run<GRAD, T0>(P.layer[0], rc, R, acc, stride);
