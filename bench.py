@@ -51,13 +51,13 @@ UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
 # capture of the timed synth_grid_runs_kernel<1,2,1301> launch at 512^3
-# (2.67 MB + 2,361.14 MB over 134,217,728 samples)
-TRAFFIC_PER_SAMPLE_FUSED = 2363.81e6 / 134217728
+# (6.32 MB + 2,391.96 MB over 134,217,728 samples)
+TRAFFIC_PER_SAMPLE_FUSED = 2398.28e6 / 134217728
 # FP32 operations executed per sample by the fused grid kernel (FFMA x 2,
 # FFMA2 x 4, FADD, FMUL per thread instruction) and its thread instructions per
 # sample, from the ncu instruction counts of the same capture
-EXEC_FP32_PER_SAMPLE_FUSED = 500.0
-INSTR_PER_SAMPLE_FUSED = 752.3
+EXEC_FP32_PER_SAMPLE_FUSED = 494.7
+INSTR_PER_SAMPLE_FUSED = 737.1
 
 
 def workload_config(grid: int, n: int) -> dict:
@@ -671,7 +671,7 @@ def run_ours(args) -> None:
                      "traffic": TRAFFIC_PER_SAMPLE_FUSED * N,
                      "traffic_source": "dram read+write of the timed synth_grid_runs_kernel<1,2,1301> launch from one ncu "
                                        f"capture of this workload at 512^3 ({TRAFFIC_PER_SAMPLE_FUSED:.2f} B/sample: writes of 16 B "
-                                       "per sample and about 10 % more, no re-reads), per sample times this launch's samples",
+                                       "per sample and about 12 % more, no re-reads), per sample times this launch's samples",
                      "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x {max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)",
                      "flops_per_sample": W.FLOPS_PER_SAMPLE_C2,
                      "flops_definition": "value path, counted by the oracle's operation-counting FP32 scalar (FMA = 2)",
