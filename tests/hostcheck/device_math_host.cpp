@@ -282,5 +282,108 @@ void hc_fastdiv(uint32_t d, const uint32_t *n, uint64_t count, uint32_t *q) {
 	const FastDiv f = FastDiv::of(d);
 	for (uint64_t i = 0; i < count; i++) q[i] = f.div(n[i]);
 }
+
+// Warp-wide pruning of the cellular table (the helpers of up_grid_runs.cuh
+// that cellular_subrun uses), checked against the unpruned search: random
+// warps of 32 lanes (table cells ty, tz in 1 .. t*max, fractions fy, fz) and
+// sub-runs of 8 samples along x, table entries made by cell_entry from
+// random hashes; every lane and sample ranks its candidates by the kernel's
+// keys (metric bits with the entry id in the low 6 bits) over the lane's 3 x 3
+// window and the columns of its x cell, once over every entry and once over
+// the entries the pruning keeps. spread: the sub-run's extent along x, and
+// lane_spread the lanes' extent along y and z, in cells (at most 1 each).
+// Returns the number of (lane, sample) pairs whose two keys differ; *kept
+// and *total count the kept and the present entries over all trials.
+int hc_prune_check(uint32_t seed, int trials, double spread, double lane_spread, uint64_t *kept, uint64_t *total) {
+	constexpr int S = 8;
+	uint32_t st = seed * 2654435761u + 12345u;
+	auto next = [&]() { st = mix32(st + 0x9E3779B9u); return st; };
+	auto unit = [&]() { return (float)(next() >> 8) * (1.0f / 16777216.0f); }; // [0, 1)
+	int bad = 0;
+	*kept = 0; *total = 0;
+	for (int t = 0; t < trials; t++) {
+		// the sub-run's x positions in the first column frame: increasing, below 2
+		const float x0 = unit(), dx = unit() * (float)spread / S;
+		float sx[S];
+		int split = S;
+		for (int r = 0; r < S; r++) {
+			const float x = x0 + dx * (float)r;
+			sx[r] = x < 1.f ? x : 1.f + (x - 1.f); // cell ixa + 1 from x = 1 on
+			if (x >= 1.f && split == S) split = r;
+		}
+		const int ncol = split < S ? 4 : 3;
+		// the lanes' cells and fractions along y and z, table cells counted from
+		// the lowest lane cell (which is table cell 1), as in cellular_subrun
+		int ty[32], tz[32];
+		float fy[32], fz[32];
+		const float y0 = unit(), z0 = unit();
+		int iymin = 2, izmin = 2;
+		for (int l = 0; l < 32; l++) {
+			const float ly = y0 + unit() * (float)lane_spread, lz = z0 + unit() * (float)lane_spread;
+			const float fly = floorf(ly), flz = floorf(lz);
+			ty[l] = (int)fly; tz[l] = (int)flz;
+			fy[l] = ly - fly; fz[l] = lz - flz;
+			iymin = ty[l] < iymin ? ty[l] : iymin;
+			izmin = tz[l] < izmin ? tz[l] : izmin;
+		}
+		int tymax = 1, tzmax = 1;
+		for (int l = 0; l < 32; l++) {
+			ty[l] += 1 - iymin; tz[l] += 1 - izmin;
+			tymax = ty[l] > tymax ? ty[l] : tymax;
+			tzmax = tz[l] > tzmax ? tz[l] : tzmax;
+		}
+		CellEntry ce[64];
+		for (int e = 0; e < 64; e++) ce[e] = cell_entry(next(), e);
+		// the warp's box and the pruning, as cellular_subrun forms them
+		CellBox box;
+		box.x0 = sx[0]; box.x1 = sx[0];
+		for (int r = 1; r < S; r++) { box.x0 = fminf(box.x0, sx[r]); box.x1 = fmaxf(box.x1, sx[r]); }
+		box.y0 = box.z0 = 3e38f; box.y1 = box.z1 = -3e38f;
+		for (int l = 0; l < 32; l++) {
+			const float ly = (float)ty[l] + fy[l], lz = (float)tz[l] + fz[l];
+			box.y0 = fminf(box.y0, ly); box.y1 = fmaxf(box.y1, ly);
+			box.z0 = fminf(box.z0, lz); box.z1 = fmaxf(box.z1, lz);
+		}
+		const int n = ncol * 16;
+		float lb[64], ub[64];
+		float u1 = 3e38f, u2 = 3e38f; // the two smallest ub of the entries seen everywhere
+		for (int e = 0; e < n; e++) {
+			cell_box_bounds<0>(ce[e], box, lb[e], ub[e]);
+			if (!cell_entry_everywhere(e, ncol, tymax, tzmax)) continue;
+			if (ub[e] < u1) { u2 = u1; u1 = ub[e]; }
+			else if (ub[e] < u2) u2 = ub[e];
+		}
+		const float thr = cell_prune_bound(u2);
+		bool keep[64];
+		for (int e = 0; e < n; e++) {
+			keep[e] = lb[e] <= thr && cell_entry_in_some_window(e, tymax, tzmax);
+			*kept += keep[e];
+			*total += 1;
+		}
+		// every lane and sample: the full search and the pruned one
+		for (int l = 0; l < 32; l++) {
+			const float tyf = (float)ty[l], tzf = (float)tz[l];
+			for (int r = 0; r < S; r++) {
+				uint32_t K[2][2] = {{0xFFFFFFFFu, 0xFFFFFFFFu}, {0xFFFFFFFFu, 0xFFFFFFFFu}};
+				for (int e = 0; e < n; e++) {
+					const int col = e >> 4, yy = (e >> 2) & 3, zz = e & 3;
+					if (abs(yy - ty[l]) > 1 || abs(zz - tz[l]) > 1) continue;    // outside the lane's window
+					if ((col == 0 && r >= split) || (col == 3 && r < split)) continue; // outside the sample's columns
+					const float vy = (ce[e].jy - tyf) - fy[l];
+					const float vz = (ce[e].jz - tzf) - fz[l];
+					const float d = cell_metric<0>(ce[e].jx - sx[r], vy * vy + vz * vz, fabsf(vy) + fabsf(vz));
+					const uint32_t k = (f_bits(d) & ~63u) | (uint32_t)e;
+					for (int v = 0; v < 2; v++) {
+						if (v == 1 && !keep[e]) continue;
+						K[v][1] = umin32(K[v][1], umax32(K[v][0], k));
+						K[v][0] = umin32(K[v][0], k);
+					}
+				}
+				if (K[0][0] != K[1][0] || K[0][1] != K[1][1]) bad++;
+			}
+		}
+	}
+	return bad;
+}
 }
 

@@ -421,3 +421,21 @@ def test_pointer_placement_rule(H):
     assert H.hc_ptr_kind(1, 1, 0, 0) == HOST       # page-locked host memory
     assert H.hc_ptr_kind(1, 0, -2, 0) == HOST      # unregistered host memory
     assert H.hc_ptr_kind(0, 2, 0, 0) == HOST       # the query failed: treated as host memory
+
+
+@pytest.mark.parametrize("spread,lane_spread", [(0.35, 0.35), (0.9, 0.15), (1.0, 1.0)])
+def test_cellular_pruning_keeps_both_keys(H, spread, lane_spread):
+    """The warp-wide pruning of the cellular table (cell_box_bounds,
+    cell_entry_everywhere, cell_entry_in_some_window, cell_prune_bound of
+    up_grid_runs.cuh) never drops one of a sample's two nearest candidates:
+    over random warps, sub-runs and tables, every lane and sample keeps the
+    two keys of the unpruned search. The realistic case (a 512^3 sub-run
+    spans about 0.35 x 0.35 x 0.15 cells) keeps a small share of the entries."""
+    H.hc_prune_check.restype = C.c_int
+    H.hc_prune_check.argtypes = [C.c_uint32, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_void_p]
+    kept, total = C.c_uint64(0), C.c_uint64(0)
+    bad = H.hc_prune_check(11, 3000, spread, lane_spread, C.byref(kept), C.byref(total))
+    assert bad == 0
+    assert 0 < kept.value < total.value
+    if (spread, lane_spread) == (0.35, 0.35):
+        assert kept.value / total.value < 0.35

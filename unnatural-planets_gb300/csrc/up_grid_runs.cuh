@@ -305,6 +305,37 @@ UP_HD CellEntry cell_entry(uint32_t h, int e) {
 	return c;
 }
 
+// Warp-wide pruning of a sub-run's shared cell table (cellular_subrun). In
+// table coordinates every sample of the warp lies in the box [x0, x1] x
+// [y0, y1] x [z0, z1]: x spans the sub-run's sx (a sample's x difference to an
+// entry is jx - sx), y and z the lanes' positions ty + fy and tz + fz.
+struct CellBox { float x0, x1, y0, y1, z0, z1; };
+// the smallest (lb) and the largest (ub) metric of entry c over the box
+template<int DIST>
+UP_HD void cell_box_bounds(const CellEntry &c, const CellBox &b, float &lb, float &ub) {
+	const float ax = b.x0 - c.jx, bx = c.jx - b.x1;
+	const float ay = b.y0 - c.jy, by = c.jy - b.y1;
+	const float az = b.z0 - c.jz, bz = c.jz - b.z1;
+	const float nx = fmaxf(fmaxf(ax, bx), 0.f), ny = fmaxf(fmaxf(ay, by), 0.f), nz = fmaxf(fmaxf(az, bz), 0.f);
+	const float fx = fmaxf(-ax, -bx), fy = fmaxf(-ay, -by), fz = fmaxf(-az, -bz);
+	lb = cell_metric<DIST>(nx, ny * ny + nz * nz, ny + nz);
+	ub = cell_metric<DIST>(fx, fy * fy + fz * fz, fy + fz);
+}
+// entry e is seen by every sample: a column of both x cells (of the sub-run's
+// ncol), y and z inside every lane's 3 x 3 window (the lanes' own table cells
+// are 1 .. tymax along y and 1 .. tzmax along z)
+UP_HD bool cell_entry_everywhere(int e, int ncol, int tymax, int tzmax) {
+	const int c = e >> 4, yy = (e >> 2) & 3, zz = e & 3;
+	return c >= (ncol == 4 ? 1 : 0) && c <= 2 && yy >= tymax - 1 && yy <= 2 && zz >= tzmax - 1 && zz <= 2;
+}
+// entry e lies inside some lane's window
+UP_HD bool cell_entry_in_some_window(int e, int tymax, int tzmax) { return ((e >> 2) & 3) <= tymax + 1 && (e & 3) <= tzmax + 1; }
+// The pruning bound from ub2, the second smallest ub of the entries seen
+// everywhere: an entry whose lb exceeds it (by 0.1 % + 1e-4, far beyond FP32
+// rounding and the keys' 2^-17 quantisation) is outranked by both of those
+// entries at every sample, so it is never one of a sample's two keys.
+UP_HD float cell_prune_bound(float ub2) { return ub2 * 1.001f + 1e-4f; }
+
 // tab: the run's x table at frequency f (xtab_entry, shared by the warp)
 template<bool GRAD, int DIST, int OP>
 UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, float amp, bool ridged, uint32_t key,
@@ -400,16 +431,12 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 		}
 #ifdef __CUDA_ARCH__
 		if (TABLE) {
-			// Warp-wide pruning. Every sample of the warp lies in the box
-			// [sxmin, sxmax] x [ymin, ymax] x [zmin, zmax] (table coordinates,
-			// a sample's x difference to entry e being jx - sx). Two entries
-			// that every sample sees (its 3 x 3 x 3 neighbourhood, both x
-			// cells) bound F2 by the second smallest of their largest metric
-			// over the box (thr); an entry whose smallest metric over the box
-			// exceeds thr (by 0.1 % + 1e-4, far beyond FP32 rounding and the
-			// keys' 2^-17 quantisation) is outranked by both at every sample,
-			// so it is never one of a sample's two keys and is skipped. The
-			// surviving entries are the same for every lane (no divergence).
+			// Warp-wide pruning (CellBox and the helpers above). Two entries
+			// that every sample sees bound F2 by the second smallest of their
+			// largest metrics over the warp's box; an entry whose smallest
+			// metric over the box exceeds that bound (cell_prune_bound) is
+			// never one of a sample's two keys and is skipped. The surviving
+			// entries are the same for every lane (no divergence).
 			const uint32_t FULL = 0xFFFFFFFFu;
 			const int lane = (int)(threadIdx.x & 31);
 			float sxmin = sx[0], sxmax = sx[0];
@@ -420,22 +447,10 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			const float ymin = bits_f(__reduce_min_sync(FULL, ly)), ymax = bits_f(__reduce_max_sync(FULL, ly));
 			const float zmin = bits_f(__reduce_min_sync(FULL, lz)), zmax = bits_f(__reduce_max_sync(FULL, lz));
 			const int tymax = iymax - iymin + 1, tzmax = izmax - izmin + 1;
-			const int n = ncol * CT * CT, c_lo = ncol == 4 ? 1 : 0;
-			auto bounds = [&](int e, float &lb, float &ub) {
-				const CellEntry c = ct[e];
-				const float ax = sxmin - c.jx, bx = c.jx - sxmax;
-				const float ay = ymin - c.jy, by = c.jy - ymax;
-				const float az = zmin - c.jz, bz = c.jz - zmax;
-				const float nx = fmaxf(fmaxf(ax, bx), 0.f), ny = fmaxf(fmaxf(ay, by), 0.f), nz = fmaxf(fmaxf(az, bz), 0.f);
-				const float fx = fmaxf(-ax, -bx), fy2 = fmaxf(-ay, -by), fz2 = fmaxf(-az, -bz);
-				lb = cell_metric<DIST>(nx, ny * ny + nz * nz, ny + nz);
-				ub = cell_metric<DIST>(fx, fy2 * fy2 + fz2 * fz2, fy2 + fz2);
-			};
-			// seen by every sample: columns of both x cells, y and z inside every lane's window
-			auto everywhere = [&](int e) {
-				const int c = e >> 4, yy = (e >> 2) & 3, zz = e & 3;
-				return c >= c_lo && c <= 2 && yy >= tymax - 1 && yy <= 2 && zz >= tzmax - 1 && zz <= 2;
-			};
+			const int n = ncol * CT * CT;
+			const CellBox box = {sxmin, sxmax, ymin, ymax, zmin, zmax};
+			auto bounds = [&](int e, float &lb, float &ub) { cell_box_bounds<DIST>(ct[e], box, lb, ub); };
+			auto everywhere = [&](int e) { return cell_entry_everywhere(e, ncol, tymax, tzmax); };
 			float lb0, ub0, lb1 = 3e38f, ub1 = 3e38f;
 			const bool has1 = lane + 32 < n; // n >= 48
 			bounds(lane, lb0, ub0);
@@ -444,9 +459,8 @@ UP_HD bool cellular_subrun(const RunCtx &rc, const XTab *tab, int r0, float f, f
 			const uint32_t a1 = f_bits(fminf(u0, u1)), a2 = f_bits(fmaxf(u0, u1));
 			const uint32_t m1 = __reduce_min_sync(FULL, a1);
 			const uint32_t first = __ffs(__ballot_sync(FULL, a1 == m1)) - 1;
-			const float thr = bits_f(__reduce_min_sync(FULL, lane == (int)first ? a2 : a1)) * 1.001f + 1e-4f;
-			// entries inside some lane's window (y, z table cells 0 .. t*max + 1)
-			auto keep = [&](int e, float lb) { return lb <= thr && ((e >> 2) & 3) <= tymax + 1 && (e & 3) <= tzmax + 1; };
+			const float thr = cell_prune_bound(bits_f(__reduce_min_sync(FULL, lane == (int)first ? a2 : a1)));
+			auto keep = [&](int e, float lb) { return lb <= thr && cell_entry_in_some_window(e, tymax, tzmax); };
 			uint32_t s0 = __ballot_sync(FULL, keep(lane, lb0));
 			uint32_t s1 = __ballot_sync(FULL, has1 && keep(lane + 32, lb1));
 			// survivors of the 16 entries of column col (bits of m), all seen by
