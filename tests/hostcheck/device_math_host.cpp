@@ -283,6 +283,23 @@ void hc_fastdiv(uint32_t d, const uint32_t *n, uint64_t count, uint32_t *q) {
 	for (uint64_t i = 0; i < count; i++) q[i] = f.div(n[i]);
 }
 
+// mix32 of a ^ b against its split form (the lattice runs hash a corner as
+// mix32_tail of the x and y/z halves, each through mix32_head): out[i] = 1
+// where they agree
+void hc_mix32_split(const uint32_t *a, const uint32_t *b, uint64_t n, uint8_t *out) {
+	for (uint64_t i = 0; i < n; i++) out[i] = mix32(a[i] ^ b[i]) == mix32_tail(mix32_head(a[i]) ^ mix32_head(b[i]));
+}
+// the ridged derivative factor of the lattice runs (n != 0 ? mul_sign(k2, n)
+// : 0) against its select form (k2 for n > 0, -k2 for n < 0, 0 at n = 0):
+// out[i] = 1 where the bits agree
+void hc_ridged_sign(const float *k2, const float *nv, uint64_t n, uint8_t *out) {
+	for (uint64_t i = 0; i < n; i++) {
+		const float a = nv[i] != 0.f ? mul_sign(k2[i], nv[i]) : 0.f;
+		const float b = nv[i] > 0.f ? k2[i] : (nv[i] < 0.f ? -k2[i] : 0.f);
+		out[i] = f_bits(a) == f_bits(b);
+	}
+}
+
 // Warp-wide pruning of the cellular table (the helpers of up_grid_runs.cuh
 // that cellular_subrun uses), checked against the unpruned search: random
 // warps of 32 lanes (table cells ty, tz in 1 .. t*max, fractions fy, fz) and

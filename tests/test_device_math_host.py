@@ -439,3 +439,32 @@ def test_cellular_pruning_keeps_both_keys(H, spread, lane_spread):
     assert 0 < kept.value < total.value
     if (spread, lane_spread) == (0.35, 0.35):
         assert kept.value / total.value < 0.35
+
+
+def test_mix32_split_equals_mix32(H):
+    """mix32(a ^ b) == mix32_tail(mix32_head(a) ^ mix32_head(b)): the first
+    mixing step (x ^= x >> 16) distributes over xor, which lets the lattice
+    runs form the y/z half once per run and the x half once per face."""
+    H.hc_mix32_split.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+    r = np.random.default_rng(4)
+    a = r.integers(0, 2 ** 32, size=1 << 16, dtype=np.uint64).astype(np.uint32)
+    b = r.integers(0, 2 ** 32, size=1 << 16, dtype=np.uint64).astype(np.uint32)
+    a[:4] = [0, 0xFFFFFFFF, 0x8000, 0x10000]
+    b[:4] = [0, 0xFFFFFFFF, 0x8000, 0xFFFF]
+    out = np.zeros(len(a), np.uint8)
+    H.hc_mix32_split(a.ctypes.data, b.ctypes.data, len(a), out.ctypes.data)
+    assert out.all()
+
+
+def test_ridged_sign_flip_equals_select(H):
+    """The lattice runs' ridged derivative factor by a sign-bit flip equals
+    the select form bit for bit, zero at n = +-0 included."""
+    H.hc_ridged_sign.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+    r = np.random.default_rng(5)
+    k2 = (r.standard_normal(1 << 16) * 0.1).astype(np.float32)
+    nv = r.standard_normal(1 << 16).astype(np.float32)
+    nv[:6] = [0.0, -0.0, 1e-45, -1e-45, np.inf, -np.inf]
+    k2[:6] = [0.08, -0.08, 0.08, 0.08, -0.5, 0.5]
+    out = np.zeros(len(nv), np.uint8)
+    H.hc_ridged_sign(k2.ctypes.data, nv.ctypes.data, len(nv), out.ctypes.data)
+    assert out.all()
