@@ -64,11 +64,15 @@ UP_HD float sqrt_hd(float x) {
 	return sqrtf(x);
 #endif
 }
-// reciprocal square root: the hardware approximation on the device (a few
-// ulp), correctly rounded 1 / sqrt on the host; used for unit vectors only
+// reciprocal square root: the hardware approximation on the device
+// (rsqrt.approx, a few ulp; inputs below 2^-126 flush to 0 and give +inf, so
+// callers guard their argument with a floor far above that), correctly rounded
+// 1 / sqrt on the host; used for unit vectors only
 UP_HD float rsqrt_hd(float x) {
 #ifdef __CUDA_ARCH__
-	return rsqrtf(x);
+	float y;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
 #else
 	return 1.f / sqrtf(x);
 #endif
@@ -361,7 +365,7 @@ UP_HD float mul_sign(float x, float s) { return bits_f(f_bits(x) ^ (f_bits(s) & 
 // (Euclidean: F is the squared distance here; -v / |v| with the reciprocal
 // square root of rsqrt_hd, 1 / sqrtf on the host)
 UP_HD V3f cell_dist_grad(V3f v, float F, int dist) {
-	if (dist == 0) return v * -(F > 0.f ? rsqrt_hd(F) : 0.f);
+	if (dist == 0) return v * -(F > 1e-36f ? rsqrt_hd(F) : 0.f); // |v| <= 1e-18: no direction
 	const V3f sg = v3(signf(v.x), signf(v.y), signf(v.z));
 	if (dist == 1) return -sg;
 	return -(v * 2.f + sg);

@@ -81,7 +81,8 @@ UP_HD SMin smooth_min_d(float a, float b, float k, float ik) {
 // Lengths and their reciprocals through sqrt_hd and rsqrt_hd: the hardware
 // approximations on the device (a few ulp), and on the host sqrtf and
 // 1 / sqrtf, the correctly rounded forms the oracle's FP32 path takes.
-UP_HD float inv_len_hd(float s) { return s > 0.f ? rsqrt_hd(s) : 0.f; } // s = squared length
+// s = squared length; lengths of 1e-18 or less have no direction (0)
+UP_HD float inv_len_hd(float s) { return s > 1e-36f ? rsqrt_hd(s) : 0.f; }
 UP_HD NG torus_d(V3f p, float R, float r) {
 	const float sa = p.x * p.x + p.y * p.y;
 	const float a = sqrt_hd(sa);
