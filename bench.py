@@ -51,13 +51,13 @@ UNIT = "Gsamples/s"
 CD_TAP = 1e-3  # central-difference tap distance of the CPU reference path (unit-scale planet)
 # DRAM bytes (read + write) per sample of the fused grid kernel, from the ncu
 # capture of the timed synth_grid_runs_kernel<1,2,1301> launch at 512^3
-# (6.32 MB + 2,391.96 MB over 134,217,728 samples)
-TRAFFIC_PER_SAMPLE_FUSED = 2398.28e6 / 134217728
+# (4.96 MB + 2,390.57 MB over 134,217,728 samples)
+TRAFFIC_PER_SAMPLE_FUSED = 2395.53e6 / 134217728
 # FP32 operations executed per sample by the fused grid kernel (FFMA x 2,
 # FFMA2 x 4, FADD, FMUL per thread instruction) and its thread instructions per
 # sample, from the ncu instruction counts of the same capture
 EXEC_FP32_PER_SAMPLE_FUSED = 494.7
-INSTR_PER_SAMPLE_FUSED = 737.1
+INSTR_PER_SAMPLE_FUSED = 711.1
 
 
 def workload_config(grid: int, n: int) -> dict:
@@ -687,7 +687,7 @@ def run_ours(args) -> None:
                                    "frac": EXEC_FP32_PER_SAMPLE_FUSED * N / (t_fused * 1e-3) / 1e12 / fp32_peak,
                                    "source": "FP32 operations the fused kernel executes per sample (FFMA and FFMA2 lanes x 2, FADD, "
                                              "FMUL), from the ncu instruction counts of this workload at 512^3 (profiles/)"},
-                     "note": "the kernel is instruction-issue bound (about 83 % issue active): per sample it issues about "
+                     "note": "the kernel is instruction-issue bound (about 82 % issue active): per sample it issues about "
                              f"{INSTR_PER_SAMPLE_FUSED:.0f} thread instructions, of which the lattice hashes and face setup of the "
                              "Perlin octaves, the cellular keys (integer min/max, bit masks), addressing and control flow are "
                              "the non-FP32 share; see profiles/",                     "hbm_view": {"algorithmic_bytes": 16 * N, "achieved_gbs": 16 * N / (t_fused * 1e-3) / 1e9,
